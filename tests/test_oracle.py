@@ -1,0 +1,134 @@
+"""Pins the CPU oracle (oracle/) against the reference's own outputs.
+
+The fixtures in tests/golden were produced by FastTools2D's MEX sources
+compiled unchanged (tests/golden/make_golden.py).  The reference's MATLAB
+tests (PE/tests/*.m) only print errors; here the same properties are
+asserted: direct-sum agreement (direct_sums_test.m), the stresslet identity
+(stresslet_identity_test.m) and parameter / replication invariance
+(consistency_test.m).
+"""
+import numpy as np
+import pytest
+from scipy.special import exp1
+
+from conftest import golden_names, relerr
+from oracle import direct, drivers
+from oracle import oracle as O
+
+# The oracle and the reference run the same algorithm; they differ only in
+# floating-point summation order and FFT implementation.
+PIN_TOL = 1e-13
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_reference(golden, name):
+    g = golden(name)
+    ps, pt, f, n = g["psrc"], g["ptar"], g["f"], g["n"]
+    a = dict(xi=g["xi"], Lx=g["Lx"], Ly=g["Ly"])
+    ur = O.mex_stokes_slp_real(ps, pt, f, g["xi"], g["nside_x"], g["nside_y"], g["Lx"], g["Ly"])
+    assert relerr(ur, g["out_slp_real"]) < PIN_TOL
+    uk = O.mex_stokes_slp_kspace(ps, pt, g["xi"], g["eta"], f, g["Mx"], g["My"], g["Lx"],
+                                 g["Ly"], g["w"], g["P"])
+    assert relerr(uk, g["out_slp_kspace"]) < PIN_TOL
+    dr = O.mex_stokes_dlp_real(ps, pt, f, n, g["xi"], g["nside_x"], g["nside_y"], g["Lx"],
+                               g["Ly"])
+    assert relerr(dr, g["out_dlp_real"]) < PIN_TOL
+    dk = O.mex_stokes_dlp_kspace(ps, pt, g["xi"], g["eta"], f, n, g["Mx"], g["My"], g["Lx"],
+                                 g["Ly"], g["w"], g["P"])
+    assert relerr(dk, g["out_dlp_kspace"]) < PIN_TOL
+    del a
+
+
+def test_pade_e1_accuracy_per_regime():
+    """The reference's E1 split: near (x <= 1) and mid (1 < x < 16) Pade forms are
+    accurate to a few ulp; the 4th-order far form (x >= 16) only to ~3e-11
+    relative at x = 80, harmless since those terms carry a factor e^-x < 1e-7."""
+    for lo, hi, tol in ((1e-8, 1.0, 4e-15), (1.0, 16.0, 4e-15), (16.0, 80.0, 5e-11)):
+        xs = np.geomspace(lo, hi, 400) if lo < 1 else np.linspace(lo, hi, 400)
+        for v in xs:
+            y, e = O.e1(v)
+            assert abs(y - exp1(v)) <= tol * exp1(v)
+            assert abs(e - np.exp(-v)) <= 4e-16 * np.exp(-v)
+
+
+def test_find_closest_node_snap():
+    h, P = 1.0 / 64, 24
+    for k in range(-32, 32):
+        x = -0.5 + (k + 32) * h
+        for dx in (0.0, 3e-14, -3e-14):
+            mx, my, px, py = O.find_closest_node(x + dx, x, 1.0, 1.0, h, P)
+            assert px == 0.0 and py == 0.0
+            assert mx == k + 32 - P // 2 and my == k + 32 - P // 2
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+def test_reference_vs_direct_sums(golden, kind):
+    """direct_sums_test.m: MEX parts vs MATLAB direct sums (N=10, Lx=1, Ly=2, tol=1e-16)."""
+    g = golden("direct_" + kind)
+    real, ks = g[f"out_{kind}_real"], g[f"out_{kind}_kspace"]
+    if kind == "dlp":
+        ks = ks - O.dlp_zero_mode(g["raw_src"], g["f"], g["n"], g["Lx"], g["Ly"])[:, None]
+    assert relerr(real, g[f"out_{kind}_real_ds"]) < 1e-12
+    assert relerr(ks, g[f"out_{kind}_kspace_ds"]) < 1e-12
+
+
+def test_cfg1_total_vs_direct_lattice_sum(golden):
+    """Config 1 SLP at xi=19.2, rc=0.25, M=64, P=24 meets its ~1e-10 tolerance."""
+    g = golden("cfg1")
+    ps, f = g["psrc"], g["f"]
+    ds = direct.slp_real_ds(ps[0], ps[1], ps[0], ps[1], f[0], f[1], 1.0, 1.0, g["xi"]) + \
+        direct.slp_kspace_ds(ps[0], ps[1], ps[0], ps[1], f[0], f[1], 1.0, 1.0, g["xi"])
+    se = g["out_slp_real"] + g["out_slp_kspace"]
+    assert relerr(se, ds) < 1e-10
+
+
+def _driver_eval(kind, xs, xt, f, n, Lx, Ly, **kw):
+    d = drivers.params(kind, xs.shape[1], xt.shape[1],
+                       float(np.sum(f ** 2)), Lx, Ly, **kw)
+    args = (d["xi"], d["nside_x"], d["nside_y"], d["Mx"], d["My"], Lx, Ly, d["P"])
+    if kind == "slp":
+        return O.slp_ewald(xs, xt, f, *args)[0]
+    return O.dlp_ewald(xs, xt, f, n, *args)[0]
+
+
+def test_stresslet_identity():
+    """stresslet_identity_test.m: density e_i on a circle -> u = e_i inside, 0 outside."""
+    r, L, ns, nt = 1.0, 4.0, 256, 16
+    hs = 2 * np.pi / ns
+    th = hs * np.arange(1, ns + 1)
+    xs = np.vstack([r * np.cos(th), r * np.sin(th)])
+    n = np.vstack([np.cos(th), np.sin(th)])
+    tt = 2 * np.pi / nt * np.arange(1, nt + 1)
+    xt = np.hstack([0.5 * r * np.vstack([np.cos(tt), np.sin(tt)]),
+                    1.5 * r * np.vstack([np.cos(tt), np.sin(tt)])])
+    for comp in (0, 1):
+        f = np.zeros((2, ns))
+        f[comp] = hs
+        u = _driver_eval("dlp", xs, xt, f, n, L, L)
+        e = np.zeros((2, 1))
+        e[comp] = 1.0
+        assert np.abs(u[:, :nt] - e).max() < 1e-9
+        assert np.abs(u[:, nt:]).max() < 1e-9
+
+
+def test_consistency_nb_and_replication():
+    """consistency_test.m: invariance to Nb (rc, xi, M) and to periodic replication."""
+    rng = np.random.default_rng(7)
+    N, Lx, Ly = 1500, 1.0, 2.0
+    f = 10 * rng.random((2, N))
+    n1 = rng.random(N)
+    n = np.vstack([n1, np.sqrt(1 - n1 ** 2)])
+    xs = np.vstack([Lx * rng.random(N), Ly * rng.random(N)])
+    xt = np.vstack([Lx * rng.random(N), Ly * rng.random(N)])
+    for kind in ("slp", "dlp"):
+        us = [_driver_eval(kind, xs, xt, f, n, Lx, Ly, Nb=nb, tol=1e-12) for nb in (9, 27)]
+        assert relerr(us[0], us[1]) < 1e-9
+        # replicate the cell along x: Lx -> 2 Lx with duplicated sources
+        xs2 = np.hstack([xs, xs + np.array([[Lx], [0.0]])])
+        f2, n2 = np.hstack([f, f]), np.hstack([n, n])
+        u1 = _driver_eval(kind, xs, xt, f, n, Lx, Ly, tol=1e-12)
+        u2 = _driver_eval(kind, xs2, xt, f2, n2, 2 * Lx, Ly, tol=1e-12)
+        if kind == "dlp":   # the zero mode depends on source locations (consistency_test.m:149-168)
+            u1 = u1 - O.dlp_zero_mode(xs, f, n, Lx, Ly)[:, None]
+            u2 = u2 - O.dlp_zero_mode(xs2, f2, n2, 2 * Lx, Ly)[:, None]
+        assert relerr(u1, u2) < 1e-9
