@@ -1,0 +1,692 @@
+// se2p_api.cu -- C ABI of libse2p (include/se2p.h): argument checks, device
+// workspace, staging of host arrays, cuFFT plans and the order of kernel
+// launches for each entry point.
+//
+// One evaluation runs as
+//   [wrap] -> sort sources/targets into boxes -> per-source coefficients
+//   -> real space (k_real)                     \  both read the sorted data
+//   -> spread -> D2Z -> filter -> Z2D -> gather /
+//   -> [DLP zero mode] -> assemble in the caller's target order.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/se2p.h"
+#include "se2p_internal.cuh"
+
+using namespace se2p;
+
+namespace {
+
+enum Slot {
+    S_IN_PS, S_IN_PT, S_IN_F, S_IN_FD, S_IN_N,   // staged inputs
+    S_WPS, S_WPT,                               // wrapped positions
+    S_SBOX, S_SRANK, S_TBOX, S_TRANK, S_COUNT,  // binning scratch
+    S_SSTART, S_TSTART, S_SPERM, S_TPERM, S_TBOXS,
+    S_SP, S_TP, S_COEF,                         // sorted data
+    S_UR_SLP, S_UR_DLP, S_UK,                   // partial results (sorted order)
+    S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM,
+    S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
+    S_COUNT_SLOTS
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct se2p_plan_st {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    DevBuf buf[S_COUNT_SLOTS];
+    std::map<std::tuple<int, int, int, int>, cufftHandle> ffts;  // (Mx, My, batch, dir)
+};
+
+namespace {
+
+int fail(se2p_plan pl, int code, const char *fmt, ...)
+{
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    if (pl) pl->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail(pl, SE2P_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+    } while (0)
+
+#define CKF(call)                                                                       \
+    do {                                                                                \
+        cufftResult r_ = (call);                                                        \
+        if (r_ != CUFFT_SUCCESS) return fail(pl, SE2P_ERR_CUFFT, "%s: cufft error %d", #call, (int)r_); \
+    } while (0)
+
+#define CKS(call)                       \
+    do {                                \
+        int s_ = (call);                \
+        if (s_ != SE2P_OK) return s_;   \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int ensure(se2p_plan pl, int slot, size_t bytes, void **out)
+{
+    DevBuf &b = pl->buf[slot];
+    if (bytes == 0) bytes = 16;
+    if (b.bytes < bytes) {
+        if (b.p) {
+            CK(cudaStreamSynchronize(pl->stream));
+            CK(cudaFree(b.p));
+            b.p = nullptr;
+            b.bytes = 0;
+        }
+        size_t want = bytes + bytes / 8;  // headroom for slightly larger calls
+        cudaError_t e = cudaMalloc(&b.p, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(pl, SE2P_ERR_ALLOC, "cudaMalloc(%zu bytes): %s", want, cudaGetErrorString(e));
+        }
+        b.bytes = want;
+    }
+    *out = b.p;
+    return SE2P_OK;
+}
+
+template <class T>
+int ensure_t(se2p_plan pl, int slot, size_t count, T **out)
+{
+    void *p = nullptr;
+    int s = ensure(pl, slot, count * sizeof(T), &p);
+    *out = static_cast<T *>(p);
+    return s;
+}
+
+// Device memory of this plan's device, aligned for 16-byte loads?
+bool device_ready(const se2p_plan pl, const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const bool dev = at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    return dev && at.device == pl->device && (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+
+// Input array of `count` double2: use in place when it is usable device
+// memory, otherwise copy it into workspace slot `slot`.
+int stage_in(se2p_plan pl, int slot, const double *p, int64_t count, const double2 **out,
+             bool *host_io)
+{
+    *out = nullptr;
+    if (count <= 0 || !p) return SE2P_OK;
+    if (device_ready(pl, p)) {
+        *out = reinterpret_cast<const double2 *>(p);
+        return SE2P_OK;
+    }
+    double2 *d = nullptr;
+    CKS(ensure_t(pl, slot, (size_t)count, &d));
+    CK(cudaMemcpyAsync(d, p, sizeof(double2) * (size_t)count, cudaMemcpyDefault, pl->stream));
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type != cudaMemoryTypeDevice &&
+        at.type != cudaMemoryTypeManaged)
+        *host_io = true;
+    cudaGetLastError();
+    *out = d;
+    return SE2P_OK;
+}
+
+// Output array: write directly into usable device memory, else into a slot
+// that is copied back by finish_out().
+struct OutBuf {
+    double *user = nullptr;
+    double2 *dev = nullptr;
+    int64_t count = 0;
+    bool staged = false;
+};
+
+int stage_out(se2p_plan pl, int slot, double *user, int64_t count, OutBuf *o, bool *host_io)
+{
+    o->user = user;
+    o->count = count;
+    o->dev = nullptr;
+    o->staged = false;
+    if (!user || count <= 0) return SE2P_OK;
+    if (device_ready(pl, user)) {
+        o->dev = reinterpret_cast<double2 *>(user);
+        return SE2P_OK;
+    }
+    CKS(ensure_t(pl, slot, (size_t)count, &o->dev));
+    o->staged = true;
+    *host_io = true;
+    return SE2P_OK;
+}
+
+int finish_out(se2p_plan pl, const OutBuf &o)
+{
+    if (o.staged && o.count > 0)
+        CK(cudaMemcpyAsync(o.user, o.dev, sizeof(double2) * (size_t)o.count, cudaMemcpyDefault,
+                           pl->stream));
+    return SE2P_OK;
+}
+
+int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
+{
+    auto key = std::make_tuple(Mx, My, batch, dir);
+    auto it = pl->ffts.find(key);
+    if (it != pl->ffts.end()) {
+        *h = it->second;
+        CKF(cufftSetStream(*h, pl->stream));
+        return SE2P_OK;
+    }
+    int n[2] = {Mx, My};
+    const int real_dist = Mx * My, cplx_dist = Mx * (My / 2 + 1);
+    cufftHandle p;
+    if (dir == 0)
+        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, CUFFT_D2Z, batch));
+    else
+        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, CUFFT_Z2D, batch));
+    CKF(cufftSetStream(p, pl->stream));
+    pl->ffts[key] = p;
+    *h = p;
+    return SE2P_OK;
+}
+
+// --------------------------------------------------------------------------
+// Argument checks (the MEX gateways' checks plus this library's limits)
+// --------------------------------------------------------------------------
+bool finite_pos(double v) { return std::isfinite(v) && v > 0; }
+
+int check_common(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar, int64_t nt,
+                 double xi, double Lx, double Ly, const double *u)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    if (ns < 0 || nt < 0) return fail(pl, SE2P_ERR_ARG, "negative point count");
+    if (ns > 0x7fffffff || nt > 0x7fffffff)
+        return fail(pl, SE2P_ERR_UNSUPPORTED, "more than 2^31-1 points");
+    if ((ns > 0 && !psrc) || (nt > 0 && !ptar)) return fail(pl, SE2P_ERR_ARG, "null point array");
+    if (nt > 0 && !u) return fail(pl, SE2P_ERR_ARG, "null output array");
+    if (!finite_pos(xi)) return fail(pl, SE2P_ERR_ARG, "xi must be positive and finite");
+    if (!finite_pos(Lx) || !finite_pos(Ly)) return fail(pl, SE2P_ERR_ARG, "Lx, Ly must be positive");
+    return SE2P_OK;
+}
+
+int check_real(se2p_plan pl, int nx, int ny)
+{
+    if (nx < 1 || ny < 1) return fail(pl, SE2P_ERR_ARG, "nside_x, nside_y must be >= 1");
+    if ((int64_t)nx * ny > (1 << 26)) return fail(pl, SE2P_ERR_UNSUPPORTED, "more than 2^26 boxes");
+    return SE2P_OK;
+}
+
+int check_kspace(se2p_plan pl, double eta, int Mx, int My, double w, int P)
+{
+    if (Mx < 2 || My < 2) return fail(pl, SE2P_ERR_ARG, "Mx, My must be >= 2");
+    if ((Mx & 1) || (My & 1))
+        return fail(pl, SE2P_ERR_UNSUPPORTED, "odd grid sizes are not supported (Mx=%d My=%d)", Mx, My);
+    if ((int64_t)Mx * My > ((int64_t)1 << 30)) return fail(pl, SE2P_ERR_UNSUPPORTED, "grid larger than 2^30 nodes");
+    if (P < 0 || (P & 1)) return fail(pl, SE2P_ERR_ARG, "P must be even and >= 0");
+    if (P > kMaxP) return fail(pl, SE2P_ERR_UNSUPPORTED, "P > %d is not supported", kMaxP);
+    if (!std::isfinite(eta) || eta <= 0) return fail(pl, SE2P_ERR_ARG, "eta must be positive");
+    if (!std::isfinite(w)) return fail(pl, SE2P_ERR_ARG, "w must be finite");
+    return SE2P_OK;
+}
+
+// --------------------------------------------------------------------------
+// The evaluation pipeline
+// --------------------------------------------------------------------------
+struct Job {
+    bool slp = false, dlp = false;     // which kernels
+    bool real = false, kspace = false; // which parts
+    bool wrap = false;                 // wrap points first (driver composites)
+    bool zero_mode = false;            // DLP k=0 term
+    double xi = 0, eta = 0, w = 0, Lx = 0, Ly = 0;
+    int nx = 1, ny = 1, Mx = 0, My = 0, P = 0;
+};
+
+struct Io {
+    const double *psrc = nullptr, *ptar = nullptr, *f_slp = nullptr, *f_dlp = nullptr,
+                 *nrm = nullptr;
+    int64_t ns = 0, nt = 0;
+    // outputs: per kind, the total u and optionally the parts
+    double *u_slp = nullptr, *ur_slp = nullptr, *uk_slp = nullptr;
+    double *u_dlp = nullptr, *ur_dlp = nullptr, *uk_dlp = nullptr;
+    int mode_slp = 0, mode_dlp = 1;   // k_assemble modes
+};
+
+int run(se2p_plan pl, const Job &J, const Io &io)
+{
+    DeviceGuard guard(pl->device);
+    cudaStream_t st = pl->stream;
+    bool host_io = false;
+    const int64_t ns = io.ns, nt = io.nt;
+
+    const double2 *ps = nullptr, *pt = nullptr, *fs = nullptr, *fd = nullptr, *nr = nullptr;
+    CKS(stage_in(pl, S_IN_PS, io.psrc, ns, &ps, &host_io));
+    CKS(stage_in(pl, S_IN_PT, io.ptar, nt, &pt, &host_io));
+    if (J.slp) CKS(stage_in(pl, S_IN_F, io.f_slp, ns, &fs, &host_io));
+    if (J.dlp) {
+        CKS(stage_in(pl, S_IN_FD, io.f_dlp, ns, &fd, &host_io));
+        CKS(stage_in(pl, S_IN_N, io.nrm, ns, &nr, &host_io));
+    }
+    OutBuf o_us, o_urs, o_uks, o_ud, o_urd, o_ukd;
+    CKS(stage_out(pl, S_OUT0, io.u_slp, nt, &o_us, &host_io));
+    CKS(stage_out(pl, S_OUT1, io.u_dlp, nt, &o_ud, &host_io));
+    // Parts are rarely requested; they share two extra slots per kind.
+    CKS(stage_out(pl, S_OUT2, io.ur_slp ? io.ur_slp : io.ur_dlp, nt, io.ur_slp ? &o_urs : &o_urd, &host_io));
+    CKS(stage_out(pl, S_OUT3, io.uk_slp ? io.uk_slp : io.uk_dlp, nt, io.uk_slp ? &o_uks : &o_ukd, &host_io));
+    if (io.ur_slp && io.ur_dlp) return fail(pl, SE2P_ERR_ARG, "internal: both part outputs requested");
+
+    if (nt == 0) return SE2P_OK;
+
+    // Wrapped positions (driver composites); the raw sources stay for the zero mode.
+    const double2 *ws = ps, *wt = pt;
+    if (J.wrap) {
+        double2 *a = nullptr, *b = nullptr;
+        if (ns > 0) {
+            CKS(ensure_t(pl, S_WPS, (size_t)ns, &a));
+            CK(launch_wrap(ns, ps, J.Lx, J.Ly, a, st, pl->launches));
+            ws = a;
+        }
+        CKS(ensure_t(pl, S_WPT, (size_t)nt, &b));
+        CK(launch_wrap(nt, pt, J.Lx, J.Ly, b, st, pl->launches));
+        wt = b;
+    }
+
+    // Boxes: the real-space cell list when the real part runs, otherwise
+    // tiles of about 16 grid cells (locality only).
+    int nx = J.nx, ny = J.ny;
+    if (!J.real) {
+        nx = J.Mx / 16 > 1 ? J.Mx / 16 : 1;
+        ny = J.My / 16 > 1 ? J.My / 16 : 1;
+    }
+    const int nbox = nx * ny;
+    int *sbox, *srank, *tbox, *trank, *count, *sstart, *tstart, *sperm, *tperm, *tboxs;
+    double2 *sp, *tp;
+    const size_t nsz = (size_t)(ns > 0 ? ns : 1), ntz = (size_t)nt;
+    CKS(ensure_t(pl, S_SBOX, nsz, &sbox));
+    CKS(ensure_t(pl, S_SRANK, nsz, &srank));
+    CKS(ensure_t(pl, S_TBOX, ntz, &tbox));
+    CKS(ensure_t(pl, S_TRANK, ntz, &trank));
+    CKS(ensure_t(pl, S_COUNT, (size_t)nbox, &count));
+    CKS(ensure_t(pl, S_SSTART, (size_t)nbox + 1, &sstart));
+    CKS(ensure_t(pl, S_TSTART, (size_t)nbox + 1, &tstart));
+    CKS(ensure_t(pl, S_SPERM, nsz, &sperm));
+    CKS(ensure_t(pl, S_TPERM, ntz, &tperm));
+    CKS(ensure_t(pl, S_TBOXS, ntz, &tboxs));
+    CKS(ensure_t(pl, S_SP, nsz, &sp));
+    CKS(ensure_t(pl, S_TP, ntz, &tp));
+
+    BinArgs bs{ws, ns, J.Lx, J.Ly, nx, ny, sbox, srank, count};
+    CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, st, pl->launches));
+    BinArgs bt{wt, nt, J.Lx, J.Ly, nx, ny, tbox, trank, count};
+    CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, st, pl->launches));
+
+    const int nc = (J.slp ? 2 : 0) + (J.dlp ? 3 : 0);
+    const int doff = J.slp ? 2 : 0;
+    double *coef = nullptr;
+    CKS(ensure_t(pl, S_COEF, (size_t)nc * nsz, &coef));
+    CK(launch_src_coef(ns, sperm, J.slp ? fs : nullptr, J.dlp ? fd : nullptr, nr, coef, nc, st,
+                       pl->launches));
+
+    double2 *ur_slp = nullptr, *ur_dlp = nullptr, *uk = nullptr;
+    if (J.real) {
+        if (J.slp) CKS(ensure_t(pl, S_UR_SLP, ntz, &ur_slp));
+        if (J.dlp) CKS(ensure_t(pl, S_UR_DLP, ntz, &ur_dlp));
+        RealArgs ra;
+        ra.sp = sp;
+        ra.coef = coef;
+        ra.nc = nc;
+        ra.doff = doff;
+        ra.sstart = sstart;
+        ra.tp = tp;
+        ra.tbox = tboxs;
+        ra.ntar = nt;
+        ra.nx = nx;
+        ra.ny = ny;
+        ra.Lx = J.Lx;
+        ra.Ly = J.Ly;
+        ra.xi = J.xi;
+        ra.xi2 = J.xi * J.xi;
+        ra.cut2 = J.Lx * J.Ly / nx / ny;                 // mex_stokes_slp_real.cpp:127
+        ra.self_c = -1.288607832450766155 - std::log(J.xi);  // mex_stokes_slp_real.cpp:124
+        ra.u_slp = ur_slp;
+        ra.u_dlp = ur_dlp;
+        CK(launch_real(ra, J.slp, J.dlp, st, pl->launches));
+    }
+
+    if (J.kspace) {
+        const int Mx = J.Mx, My = J.My, P = J.P;
+        const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
+        const int nout = (J.slp ? 2 : 0) + (J.dlp ? 2 : 0);
+        const double h = J.Lx / Mx;
+        double *grid = nullptr, *e1 = nullptr;
+        cufftDoubleComplex *spec = nullptr;
+        CKS(ensure_t(pl, S_GRID, G * nc, &grid));
+        CKS(ensure_t(pl, S_SPEC, H * nc, &spec));
+        CKS(ensure_t(pl, S_E1, (size_t)P + 1, &e1));
+        CKS(ensure_t(pl, S_UK, ntz * (nout / 2), &uk));
+        // e1[j] = exp(-2 xi^2/eta h^2 j^2) (mex_stokes_slp_kspace.cpp:64-67)
+        double e1h[kMaxP + 1];
+        const double t = -2 * J.xi * J.xi / J.eta * h * h;
+        for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
+        CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * nc, st));
+
+        SpreadArgs sa;
+        sa.sp = sp;
+        sa.coef = coef;
+        sa.ns = ns;
+        sa.grid = grid;
+        sa.Mx = Mx;
+        sa.My = My;
+        sa.P = P;
+        sa.Lhx = J.Lx / 2.0;
+        sa.Lhy = J.Ly / 2.0;
+        sa.h = h;
+        sa.w = J.w;
+        sa.a = -2 * J.xi * J.xi / J.eta;
+        sa.e1 = e1;
+        CK(launch_spread(sa, nc, st, pl->launches));
+
+        cufftHandle fwd, inv;
+        CKS(get_fft(pl, Mx, My, nc, 0, &fwd));
+        CKF(cufftExecD2Z(fwd, grid, spec));
+
+        FilterArgs fa;
+        fa.spec = spec;
+        fa.Mx = Mx;
+        fa.My = My;
+        fa.Lx = J.Lx;
+        fa.Ly = J.Ly;
+        fa.xi = J.xi;
+        fa.eta = J.eta;
+        fa.scale = 1.0 / ((double)Mx * (double)My);
+        fa.slp_in = J.slp ? 0 : -1;
+        fa.dlp_in = J.dlp ? doff : -1;
+        fa.slp_out = 0;
+        fa.dlp_out = J.slp ? 2 : 0;
+        CK(launch_filter(fa, st, pl->launches));
+
+        CKS(get_fft(pl, Mx, My, nout, 1, &inv));
+        CKF(cufftExecZ2D(inv, spec, grid));
+
+        GatherArgs ga;
+        ga.tp = tp;
+        ga.nt = nt;
+        ga.grid = grid;
+        ga.Mx = Mx;
+        ga.My = My;
+        ga.P = P;
+        ga.Lhx = J.Lx / 2.0;
+        ga.Lhy = J.Ly / 2.0;
+        ga.h = h;
+        ga.w = J.w;
+        ga.a = -2 * J.xi * J.xi / J.eta;
+        double s = 4 * J.xi * J.xi / J.eta;               // mex_stokes_slp_kspace.cpp:325-328
+        s = s * s * h * h / kPi;
+        ga.scale = s / (4 * kPi);
+        ga.e1 = e1;
+        ga.out = uk;
+        CK(launch_gather(ga, nout, st, pl->launches));
+    }
+
+    double2 *zm = nullptr;
+    if (J.zero_mode && J.dlp) {
+        double2 *part = nullptr;
+        CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
+        CKS(ensure_t(pl, S_ZM, 1, &zm));
+        // sum over the caller's (unwrapped) sources
+        CK(launch_zero_mode(ns, ps, fd, nr, 1.0 / (J.Lx * J.Ly), part, zm, st, pl->launches));
+    }
+
+    const double2 *uk_slp = (J.kspace && J.slp) ? uk : nullptr;
+    const double2 *uk_dlp = (J.kspace && J.dlp) ? uk + (J.slp ? nt : 0) : nullptr;
+    if (J.slp && o_us.dev)
+        CK(launch_assemble(nt, io.mode_slp, tperm, J.real ? ur_slp : nullptr, uk_slp, nullptr,
+                           o_us.dev, o_urs.dev, o_uks.dev, st, pl->launches));
+    if (J.dlp && o_ud.dev)
+        CK(launch_assemble(nt, io.mode_dlp, tperm, J.real ? ur_dlp : nullptr, uk_dlp, zm,
+                           o_ud.dev, o_urd.dev, o_ukd.dev, st, pl->launches));
+
+    CKS(finish_out(pl, o_us));
+    CKS(finish_out(pl, o_ud));
+    CKS(finish_out(pl, o_urs));
+    CKS(finish_out(pl, o_urd));
+    CKS(finish_out(pl, o_uks));
+    CKS(finish_out(pl, o_ukd));
+    if (host_io) CK(cudaStreamSynchronize(st));
+    else CK(cudaGetLastError());
+    return SE2P_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char *se2p_version(void) { return "se2p 0.1 (sm_103a)"; }
+
+int se2p_plan_create(se2p_plan *plan, int device)
+{
+    if (!plan) return SE2P_ERR_ARG;
+    *plan = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return SE2P_ERR_CUDA;
+    }
+    se2p_plan pl = new se2p_plan_st;
+    pl->device = device;
+    DeviceGuard guard(device);
+    if (cudaStreamCreateWithFlags(&pl->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete pl;
+        return SE2P_ERR_CUDA;
+    }
+    pl->stream = pl->own;
+    *plan = pl;
+    return SE2P_OK;
+}
+
+int se2p_plan_destroy(se2p_plan pl)
+{
+    if (!pl) return SE2P_OK;
+    DeviceGuard guard(pl->device);
+    cudaStreamSynchronize(pl->stream);
+    for (auto &kv : pl->ffts) cufftDestroy(kv.second);
+    for (auto &b : pl->buf)
+        if (b.p) cudaFree(b.p);
+    if (pl->own) cudaStreamDestroy(pl->own);
+    delete pl;
+    return SE2P_OK;
+}
+
+int se2p_plan_set_stream(se2p_plan pl, void *s)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    pl->stream = static_cast<cudaStream_t>(s);   // NULL = the legacy default stream
+    return SE2P_OK;
+}
+
+const char *se2p_plan_last_error(se2p_plan pl) { return pl ? pl->err.c_str() : "null plan"; }
+
+int64_t se2p_plan_workspace_bytes(se2p_plan pl)
+{
+    if (!pl) return 0;
+    int64_t s = 0;
+    for (auto &b : pl->buf) s += (int64_t)b.bytes;
+    return s;
+}
+
+int64_t se2p_plan_kernel_launches(se2p_plan pl) { return pl ? pl->launches : 0; }
+
+int se2p_slp_real(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar, int64_t nt,
+                  const double *f, double xi, int nside_x, int nside_y, double Lx, double Ly,
+                  double *u)
+{
+    CKS(check_common(pl, psrc, ns, ptar, nt, xi, Lx, Ly, u));
+    CKS(check_real(pl, nside_x, nside_y));
+    if (ns > 0 && !f) return fail(pl, SE2P_ERR_ARG, "null f");
+    Job J;
+    J.slp = J.real = true;
+    J.xi = xi; J.Lx = Lx; J.Ly = Ly; J.nx = nside_x; J.ny = nside_y;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_slp = f; io.ns = ns; io.nt = nt;
+    io.u_slp = u; io.mode_slp = 0;
+    return run(pl, J, io);
+}
+
+int se2p_dlp_real(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar, int64_t nt,
+                  const double *f, const double *n, double xi, int nside_x, int nside_y,
+                  double Lx, double Ly, double *u)
+{
+    CKS(check_common(pl, psrc, ns, ptar, nt, xi, Lx, Ly, u));
+    CKS(check_real(pl, nside_x, nside_y));
+    if (ns > 0 && (!f || !n)) return fail(pl, SE2P_ERR_ARG, "null f or n");
+    Job J;
+    J.dlp = J.real = true;
+    J.xi = xi; J.Lx = Lx; J.Ly = Ly; J.nx = nside_x; J.ny = nside_y;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_dlp = f; io.nrm = n; io.ns = ns; io.nt = nt;
+    io.u_dlp = u; io.mode_dlp = 1;
+    return run(pl, J, io);
+}
+
+int se2p_slp_kspace(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar,
+                    int64_t nt, double xi, double eta, const double *f, int Mx, int My,
+                    double Lx, double Ly, double w, int P, double *u)
+{
+    CKS(check_common(pl, psrc, ns, ptar, nt, xi, Lx, Ly, u));
+    CKS(check_kspace(pl, eta, Mx, My, w, P));
+    if (ns > 0 && !f) return fail(pl, SE2P_ERR_ARG, "null f");
+    Job J;
+    J.slp = J.kspace = true;
+    J.xi = xi; J.eta = eta; J.w = w; J.Lx = Lx; J.Ly = Ly; J.Mx = Mx; J.My = My; J.P = P;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_slp = f; io.ns = ns; io.nt = nt;
+    io.u_slp = u; io.mode_slp = 2;
+    return run(pl, J, io);
+}
+
+int se2p_dlp_kspace(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar,
+                    int64_t nt, double xi, double eta, const double *f, const double *n, int Mx,
+                    int My, double Lx, double Ly, double w, int P, double *u)
+{
+    CKS(check_common(pl, psrc, ns, ptar, nt, xi, Lx, Ly, u));
+    CKS(check_kspace(pl, eta, Mx, My, w, P));
+    if (ns > 0 && (!f || !n)) return fail(pl, SE2P_ERR_ARG, "null f or n");
+    Job J;
+    J.dlp = J.kspace = true;
+    J.xi = xi; J.eta = eta; J.w = w; J.Lx = Lx; J.Ly = Ly; J.Mx = Mx; J.My = My; J.P = P;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_dlp = f; io.nrm = n; io.ns = ns; io.nt = nt;
+    io.u_dlp = u; io.mode_dlp = 2;
+    return run(pl, J, io);
+}
+
+static int check_params(se2p_plan pl, const se2p_params *p)
+{
+    if (!p) return fail(pl, SE2P_ERR_ARG, "null params");
+    CKS(check_real(pl, p->nside_x, p->nside_y));
+    CKS(check_kspace(pl, p->eta, p->Mx, p->My, p->w, p->P));
+    return SE2P_OK;
+}
+
+static void job_from_params(Job &J, const se2p_params *p)
+{
+    J.real = J.kspace = J.wrap = true;
+    J.xi = p->xi; J.eta = p->eta; J.w = p->w; J.Lx = p->Lx; J.Ly = p->Ly;
+    J.nx = p->nside_x; J.ny = p->nside_y; J.Mx = p->Mx; J.My = p->My; J.P = p->P;
+}
+
+int se2p_slp_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, int64_t ns,
+                   const double *ptar, int64_t nt, const double *f, double *u, double *ur,
+                   double *uk)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    CKS(check_params(pl, prm));
+    CKS(check_common(pl, psrc, ns, ptar, nt, prm->xi, prm->Lx, prm->Ly, u));
+    if (ns > 0 && !f) return fail(pl, SE2P_ERR_ARG, "null f");
+    Job J;
+    job_from_params(J, prm);
+    J.slp = true;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_slp = f; io.ns = ns; io.nt = nt;
+    io.u_slp = u; io.ur_slp = ur; io.uk_slp = uk; io.mode_slp = 3;
+    return run(pl, J, io);
+}
+
+int se2p_dlp_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, int64_t ns,
+                   const double *ptar, int64_t nt, const double *f, const double *n, double *u,
+                   double *ur, double *uk)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    CKS(check_params(pl, prm));
+    CKS(check_common(pl, psrc, ns, ptar, nt, prm->xi, prm->Lx, prm->Ly, u));
+    if (ns > 0 && (!f || !n)) return fail(pl, SE2P_ERR_ARG, "null f or n");
+    Job J;
+    job_from_params(J, prm);
+    J.dlp = true;
+    J.zero_mode = true;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_dlp = f; io.nrm = n; io.ns = ns; io.nt = nt;
+    io.u_dlp = u; io.ur_dlp = ur; io.uk_dlp = uk; io.mode_dlp = 4;
+    return run(pl, J, io);
+}
+
+int se2p_stokes_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, int64_t ns,
+                      const double *ptar, int64_t nt, const double *f_slp, const double *f_dlp,
+                      const double *n, double *u_slp, double *u_dlp)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    CKS(check_params(pl, prm));
+    CKS(check_common(pl, psrc, ns, ptar, nt, prm->xi, prm->Lx, prm->Ly, u_slp));
+    if (nt > 0 && !u_dlp) return fail(pl, SE2P_ERR_ARG, "null u_dlp");
+    if (ns > 0 && (!f_slp || !f_dlp || !n)) return fail(pl, SE2P_ERR_ARG, "null f or n");
+    Job J;
+    job_from_params(J, prm);
+    J.slp = J.dlp = true;
+    J.zero_mode = true;
+    Io io;
+    io.psrc = psrc; io.ptar = ptar; io.f_slp = f_slp; io.f_dlp = f_dlp; io.nrm = n;
+    io.ns = ns; io.nt = nt;
+    io.u_slp = u_slp; io.u_dlp = u_dlp; io.mode_slp = 3; io.mode_dlp = 4;
+    return run(pl, J, io);
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+// se2p_internal.cuh -- device helpers and kernel argument blocks shared by the
+// spectral-Ewald kernels (se2p_kernels.cu) and the host orchestration
+// (se2p_api.cu).  Everything here is sm_103a device code or plain structs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+namespace se2p {
+
+constexpr double kPi = 3.1415926535897932385;
+// Largest stencil handled: P + 1 nodes per axis must fit one warp.
+constexpr int kMaxP = 30;
+
+// ---------------------------------------------------------------------------
+// Never-contracted FP64 arithmetic.  Used wherever the reference's own
+// rounding decides a discrete outcome: the box index of a point, the
+// real-space cutoff test r2 < Lx*Ly/nside_x/nside_y and the grid-node snap.
+// The reference is built for x86 SSE (no FMA), so each product and sum is
+// rounded separately; a fused a*b+c could move a pair across the cutoff.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Box of coordinate x: clamp(floor(nside*(x/L + 0.5)), 0, nside-1)
+// (PE/src/mex/common/ewald_tools.cpp:28-33).
+__device__ __forceinline__ int box1(double x, double L, int nside)
+{
+    double t = floor(xmul((double)nside, xadd(xdiv(x, L), 0.5)));
+    int b = (int)t;  // saturating conversion; NaN -> 0, then clamped like x86's INT_MIN
+    b = b < 0 ? 0 : b;
+    return b >= nside ? nside - 1 : b;
+}
+
+// Stencil origin and in-cell offset of a point (FindClosestNode,
+// PE/src/mex/common/ewald_tools.cpp:86-114).  Node index 0 sits at -L/2.
+__device__ __forceinline__ void closest_node(double x, double y, double Lhx, double Lhy,
+                                             double h, int P, int &mx, int &my,
+                                             double &px, double &py)
+{
+    const double snap = 1e-13;
+    double ox = xsub(x, xmul(h, floor(xdiv(x, h))));
+    double oy = xsub(y, xmul(h, floor(xdiv(y, h))));
+    double tx = xdiv(xadd(x, Lhx), h);
+    double ty = xdiv(xadd(y, Lhy), h);
+    const double half = (double)(P / 2);
+    int ix = (int)xsub(floor(tx), half);
+    int iy = (int)xsub(floor(ty), half);
+    if (fabs(ox) < snap || fabs(xsub(ox, h)) < snap) ox = 0.0;
+    if (fabs(oy) < snap || fabs(xsub(oy, h)) < snap) oy = 0.0;
+    if (ox == 0.0 && remainder(xsub(tx, half), 1.0) < 0) ix++;
+    if (oy == 0.0 && remainder(xsub(ty, half), 1.0) < 0) iy++;
+    mx = ix; my = iy; px = ox; py = oy;
+}
+
+// ---------------------------------------------------------------------------
+// E1 by the reference's three-regime Pade split
+// (PE/src/mex/StokesSLP/mex_stokes_slp_real.cpp:19-47, :166-205).
+// Coefficients are numerator/denominator pairs, highest power first; Horner
+// runs in 1/x for x > 1 and in x for x <= 1.  e = exp(-x) is passed in.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double e1_pade(double x, double e)
+{
+    if (x >= 16.0) {
+        const double r = 1.0 / x;
+        double a = -17.70313744792479226930481672752649;
+        double b = -2.03222164752550948918496942496859;
+        a = fma(r, a, -9.56230625623594754358691716333851);
+        b = fma(r, b, 24.24775264986217493401454703416675);
+        a = fma(r, a, -0.99999982131078080094255255971802);
+        b = fma(r, b, 34.82867640350680460414878325536847);
+        a = fma(r, a, -0.00000000083503088648841284312372);
+        b = fma(r, b, 11.56228921223568129050818242831156);
+        return e * (r + a / (b + x));
+    } else if (x > 1.0) {
+        const double r = 1.0 / x;
+        double a = -1185.45720315201027667;
+        double b = -0.776491285282330997549;
+        a = fma(r, a, -14751.4895786128450662);
+        b = fma(r, b, 1229.20784182403048905);
+        a = fma(r, a, -54844.4587226402067411);
+        b = fma(r, b, 18455.4124737722049515);
+        a = fma(r, a, -86273.1567711649528784);
+        b = fma(r, b, 86722.3403467334749201);
+        a = fma(r, a, -66598.2652345418633509);
+        b = fma(r, b, 180329.498380501819718);
+        a = fma(r, a, -27182.6254466733970467);
+        b = fma(r, b, 192104.047790227984431);
+        a = fma(r, a, -6046.8250112711035463);
+        b = fma(r, b, 113057.05869159631492);
+        a = fma(r, a, -724.581482791462469795);
+        b = fma(r, b, 38129.5594484818471461);
+        a = fma(r, a, -43.3058660811817946037);
+        b = fma(r, b, 7417.37624454689546708);
+        a = fma(r, a, -0.999999999999998811143);
+        b = fma(r, b, 809.193214954550328455);
+        a = fma(r, a, -0.121013190657725568138e-18);
+        b = fma(r, b, 45.3058660811801465927);
+        return e * (r + a / (b + x));
+    }
+    double a = -0.000111507792921197858394;
+    double b = -0.528611029520217142048e-6;
+    a = fma(x, a, -0.00399167106081113256961);
+    b = fma(x, b, 0.000131049900798434683324);
+    a = fma(x, a, -0.0368031736257943745142);
+    b = fma(x, b, 0.00427347600017103698101);
+    a = fma(x, a, -0.245088216639761496153);
+    b = fma(x, b, 0.056770677104207528384);
+    a = fma(x, a, 0.0320913665303559189999);
+    b = fma(x, b, 0.37091387659397013215);
+    a = fma(x, a, 0.0865197248079397976498);
+    b = fma(x, b, 1.0);
+    return a / b + x - log(x) - 0.66373538970947265625;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel argument blocks
+// ---------------------------------------------------------------------------
+struct BinArgs {
+    const double2 *p;   // interleaved (x, y) per point
+    int64_t n;
+    double Lx, Ly;
+    int nx, ny;
+    int *box, *rank, *count;
+};
+
+struct RealArgs {
+    const double2 *sp;    // sources, sorted by box
+    const double *coef;   // nc coefficients per sorted source: SLP f at [0,1],
+                          // DLP S = f (x) n as (S11, S12+S21, S22) at [doff, doff+3)
+    int nc, doff;
+    const int *sstart;    // box b's sources: [sstart[b], sstart[b+1])
+    const double2 *tp;    // targets, sorted by box
+    const int *tbox;      // box of each sorted target
+    int64_t ntar;
+    int nx, ny;
+    double Lx, Ly, xi, xi2, cut2, self_c;
+    double2 *u_slp;       // raw sums per sorted target (no 1/(4 pi))
+    double2 *u_dlp;
+};
+
+struct SpreadArgs {
+    const double2 *sp;    // source positions
+    const double *coef;   // NC coefficients per source
+    int64_t ns;
+    double *grid;         // NC grids, each Mx x My with y fastest
+    int Mx, My, P;
+    double Lhx, Lhy, h, w, a;   // a = -2 xi^2 / eta
+    const double *e1;     // exp(a h^2 j^2), j = -P/2..P/2
+};
+
+struct FilterArgs {
+    cufftDoubleComplex *spec;   // component c at spec + c * Mx * (My/2+1)
+    int Mx, My;
+    double Lx, Ly, xi, eta, scale;   // scale = 1 / (Mx My)
+    int slp_in, dlp_in;         // first spectrum of each kind (-1 = absent)
+    int slp_out, dlp_out;       // where the 2 filtered spectra of each kind go
+};
+
+struct GatherArgs {
+    const double2 *tp;
+    int64_t nt;
+    const double *grid;   // NC grids (filtered, inverse transformed)
+    int Mx, My, P;
+    double Lhx, Lhy, h, w, a, scale;
+    const double *e1;
+    double2 *out;         // NC/2 outputs per target, [k * nt + t]
+};
+
+// ---------------------------------------------------------------------------
+// Host launchers (se2p_kernels.cu).  Each returns the launch status.
+// ---------------------------------------------------------------------------
+cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *sorted_box,
+                       double2 *sorted_pos, cudaStream_t st, int64_t &launches);
+cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
+                            const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
+                            cudaStream_t st, int64_t &launches);
+cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
+                        int64_t &launches);
+cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t &launches);
+cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
+cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches);
+cudaError_t launch_wrap(int64_t n, const double2 *p, double Lx, double Ly, double2 *out,
+                        cudaStream_t st, int64_t &launches);
+cudaError_t launch_zero_mode(int64_t n, const double2 *p, const double2 *f, const double2 *nrm,
+                             double inv_area, double2 *part, double2 *zm, cudaStream_t st,
+                             int64_t &launches);
+cudaError_t launch_assemble(int64_t n, int mode, const int *perm, const double2 *ur,
+                            const double2 *uk, const double2 *zm, double2 *u, double2 *ur_out,
+                            double2 *uk_out, cudaStream_t st, int64_t &launches);
+constexpr int kZeroModeParts = 304;
+
+}  // namespace se2p

@@ -1,0 +1,264 @@
+"""Driver layer: the MATLAB functions StokesSLP_ewald_2p / StokesDLP_ewald_2p of
+FastTools2D (PeriodicEwald/src/matlab/*.m) on top of libse2p.
+
+``StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None,
+tol=1e-16, verbose=False)`` returns ``(u1, u2, ur, uk, xi)`` like the MATLAB
+function; ``StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly,
+...)`` likewise.  Parameter selection (rc from Nb, xi and kinf from the
+Palsson-Tornberg error estimates by Newton iteration, M, w, eta) follows
+StokesSLP_ewald_2p.m:27-104 and :147-202, StokesDLP_ewald_2p.m:30-125 and
+:171-224, including their differences (the SLP passes Lx twice to its kinf
+estimate; the DLP kinf estimate keeps the expression k*8*pi*Q*max/Lx^3*Ly^3
+as MATLAB parses it).
+
+The lower-level ``slp_ewald``, ``dlp_ewald`` and ``stokes_ewald`` take the
+Ewald parameters directly (an :class:`EwaldParams`) and call the C ABI
+composites se2p_slp_ewald / se2p_dlp_ewald / se2p_stokes_ewald.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .mex import _Arg, _Out, _bind_stream, _plan, _same_n
+
+
+@dataclass
+class EwaldParams:
+    xi: float
+    nside_x: int
+    nside_y: int
+    Mx: int
+    My: int
+    P: int
+    Lx: float
+    Ly: float
+    w: float
+    eta: float
+
+    @staticmethod
+    def derived(xi, nside_x, nside_y, Mx, My, P, Lx, Ly):
+        """w = P Lx/Mx/2, eta = (2 xi w/m)^2 with m = 0.95 sqrt(pi P)
+        (StokesSLP_ewald_2p.m:90, :103-104)."""
+        w = P * Lx / Mx / 2
+        m = 0.95 * math.sqrt(math.pi * P)
+        return EwaldParams(float(xi), int(nside_x), int(nside_y), int(Mx), int(My), int(P),
+                           float(Lx), float(Ly), w, (2 * xi * w / m) ** 2)
+
+    def as_c(self) -> _lib.Params:
+        return _lib.Params(self.xi, self.nside_x, self.nside_y, self.Mx, self.My, self.P,
+                           self.Lx, self.Ly, self.w, self.eta)
+
+
+# ----------------------------------------------------------------------------
+# Parameter selection
+# ----------------------------------------------------------------------------
+def _round_half_away(x: float) -> float:
+    return math.floor(x + 0.5) if x >= 0 else -math.floor(-x + 0.5)
+
+
+def rational(x: float):
+    """(A, B) with A/B ~ x to 1e-6 relative by continued fractions (MATLAB rat)."""
+    tol = 1e-6 * abs(x)
+    num, den = _round_half_away(x), 1.0
+    pnum, pden = 1.0, 0.0
+    rest = x - num
+    while abs(x - num / den) >= tol:
+        inv = 1.0 / rest
+        a = _round_half_away(inv)
+        rest = inv - a
+        num, pnum = a * num + pnum, num
+        den, pden = a * den + pden, den
+    sign = -1 if den < 0 else 1
+    return int(sign * num), int(abs(den))
+
+
+def _newton_limited(g, dg, x, tol, maxit=100):
+    """x <- x - min(g/g', 0.9 x) until |g| <= tol (at most maxit+2 steps)."""
+    for _ in range(maxit + 2):
+        gx = g(x)
+        if abs(gx) <= tol:
+            break
+        x -= min(gx / dg(x), 0.9 * x)
+    return x
+
+
+def _xi_slp(Q, Lx, Ly, rc, tol):
+    c = math.sqrt(Q * math.pi / (4 * Lx * Ly))
+    g = lambda x: c / math.sqrt(x) * math.exp(-(x * rc) ** 2) - tol
+    dg = lambda x: -c * math.exp(-(x * rc) ** 2) * (0.5 * x ** -1.5 + 2 * rc * rc * math.sqrt(x))
+    return _newton_limited(g, dg, 4 / rc, tol)
+
+
+def _kinf_slp(Q, L1, L2, xi, tol):
+    c = math.sqrt(4 * Q * math.pi * max(L1, L2) / (L1 ** 3 * L2 ** 3))
+    s = 4 * xi * xi
+    g = lambda k: c / math.sqrt(k) * math.exp(-k * k / s) - tol
+    dg = lambda k: -c * math.exp(-k * k / s) * (0.5 * k ** -1.5 + 2 * math.sqrt(k) / s)
+    k = _newton_limited(g, dg, _round_half_away(5 * xi), tol)
+    return int(_round_half_away(L1 * k / (2 * math.pi)))
+
+
+def _xi_dlp(Q, Lx, Ly, rc, tol):
+    c = math.sqrt(2 * math.pi * Q / (Lx * Ly))
+    g = lambda a: math.exp(-(a * rc) ** 2) * a * rc * c - tol
+    dg = lambda a: (1 - 2 * (a * rc) ** 2) * math.exp(-(a * rc) ** 2) * c * rc
+    return _newton_limited(g, dg, 1 / rc, tol)
+
+
+def _kinf_dlp(Q, L1, L2, xi, tol):
+    # MATLAB parses sqrt(k*8*pi*Q*max(Lx,Ly)/Lx^3*Ly^3) as ((...)/Lx^3)*Ly^3.
+    c = math.sqrt(8 * math.pi * Q * max(L1, L2) / L1 ** 3 * L2 ** 3)
+    s = 4 * xi * xi
+    g = lambda k: c * math.sqrt(k) * math.exp(-k * k / s) - tol
+    dg = lambda k: c * math.exp(-k * k / s) * (0.5 / math.sqrt(k) - 2 * k ** 1.5 / s)
+    k = _newton_limited(g, dg, _round_half_away(5 * xi), tol)
+    return int(_round_half_away(L1 * k / (2 * math.pi)))
+
+
+def select_params(kind: str, nsrc: int, ntar: int, fsq_sum: float, Lx: float, Ly: float,
+                  P: int = 24, Nb=None, tol: float = 1e-16) -> EwaldParams:
+    """Ewald parameters as the MATLAB drivers choose them; fsq_sum = sum(f.^2)."""
+    npts = nsrc + ntar
+    if Nb is None:
+        Nb = min(P * _round_half_away(math.log2(npts)), npts / 4)
+    A, B = rational(Lx / Ly)
+    Q = fsq_sum + 1
+    a = math.ceil(math.sqrt(npts / (Nb * A * B)))
+    nside_x, nside_y = a * A, a * B
+    rc = Lx / nside_x
+    if kind == "slp":
+        xi = _xi_slp(Q, Lx, Ly, rc, tol)
+        kinf = _kinf_slp(Q, Lx, Lx, xi, tol)
+    elif kind == "dlp":
+        xi = _xi_dlp(Q, Lx, Ly, rc, tol)
+        kinf = _kinf_dlp(Q, Lx, Lx, xi, tol)
+    else:
+        raise ValueError("kind must be 'slp' or 'dlp'")
+    M = min(2 * kinf, 10000)
+    return EwaldParams.derived(xi, nside_x, nside_y, A * M, B * M, P, Lx, Ly)
+
+
+# ----------------------------------------------------------------------------
+# Composites with given parameters
+# ----------------------------------------------------------------------------
+def slp_ewald(psrc, ptar, f, prm: EwaldParams, parts=False, plan=None):
+    """u = ur + uk after wrapping (StokesSLP_ewald_2p.m:74-82, :119-133).
+
+    MATLAB-shaped (2, N) numpy arrays or (N, 2) CUDA tensors.  Returns u, or
+    (u, ur, uk) with parts=True."""
+    pl = _plan(plan)
+    s, t, ff = _Arg(psrc, "psrc"), _Arg(ptar, "ptar"), _Arg(f, "f")
+    _same_n(s, ff, "psrc and f must be the same size.")
+    _bind_stream(pl, t.torch)
+    outs = [_Out(t.n, t.torch, pl.device) for _ in range(3 if parts else 1)]
+    c = prm.as_c()
+    pl.check(pl.lib.se2p_slp_ewald(pl.handle, ctypes.byref(c), s.ptr, s.n, t.ptr, t.n, ff.ptr,
+                                   outs[0].ptr, outs[1].ptr if parts else None,
+                                   outs[2].ptr if parts else None))
+    r = [o.result() for o in outs]
+    return tuple(r) if parts else r[0]
+
+
+def dlp_ewald(psrc, ptar, f, n, prm: EwaldParams, parts=False, plan=None):
+    """u = -(ur + uk - sum((f.n) x_src)/(Lx Ly)) (StokesDLP_ewald_2p.m:295-360).
+    The zero-mode term uses the caller's unwrapped source positions."""
+    pl = _plan(plan)
+    s, t, ff, nn = _Arg(psrc, "psrc"), _Arg(ptar, "ptar"), _Arg(f, "f"), _Arg(n, "n")
+    _same_n(s, ff, "psrc and f must be the same size.")
+    _same_n(s, nn, "psrc and n must be the same size.")
+    _bind_stream(pl, t.torch)
+    outs = [_Out(t.n, t.torch, pl.device) for _ in range(3 if parts else 1)]
+    c = prm.as_c()
+    pl.check(pl.lib.se2p_dlp_ewald(pl.handle, ctypes.byref(c), s.ptr, s.n, t.ptr, t.n, ff.ptr,
+                                   nn.ptr, outs[0].ptr, outs[1].ptr if parts else None,
+                                   outs[2].ptr if parts else None))
+    r = [o.result() for o in outs]
+    return tuple(r) if parts else r[0]
+
+
+def stokes_ewald(psrc, ptar, f_slp, f_dlp, n, prm: EwaldParams, plan=None):
+    """(u_slp, u_dlp) on one point set in one pass (se2p_stokes_ewald)."""
+    pl = _plan(plan)
+    s, t = _Arg(psrc, "psrc"), _Arg(ptar, "ptar")
+    fs, fd, nn = _Arg(f_slp, "f_slp"), _Arg(f_dlp, "f_dlp"), _Arg(n, "n")
+    for a, nm in ((fs, "f_slp"), (fd, "f_dlp"), (nn, "n")):
+        _same_n(s, a, f"psrc and {nm} must be the same size.")
+    _bind_stream(pl, t.torch)
+    o1, o2 = _Out(t.n, t.torch, pl.device), _Out(t.n, t.torch, pl.device)
+    c = prm.as_c()
+    pl.check(pl.lib.se2p_stokes_ewald(pl.handle, ctypes.byref(c), s.ptr, s.n, t.ptr, t.n,
+                                      fs.ptr, fd.ptr, nn.ptr, o1.ptr, o2.ptr))
+    return o1.result(), o2.result()
+
+
+# ----------------------------------------------------------------------------
+# The MATLAB drivers
+# ----------------------------------------------------------------------------
+def _col(a):
+    return np.asarray(a, dtype=np.float64).reshape(-1)
+
+
+def _verbose_print(kind, prm, ns, nt, tol, Nb):
+    name = "SINGLE" if kind == "slp" else "DOUBLE"
+    print(f"SPECTRAL EWALD FOR THE STOKES {name}-LAYER POTENTIAL")
+    print(f"NUMBER OF SOURCES: {ns}\nNUMBER OF TARGETS: {nt}\nTOLERANCE: {tol:3.3e}")
+    print(f"P: {prm.P}\nPoints per box: {Nb}")
+    print(f"\txi: {prm.xi:3.3f}\n\trc: {prm.Lx / prm.nside_x:3.3f}\n\tMx: {prm.Mx}\n"
+          f"\tMy: {prm.My}\n\tw: {prm.w:3.3f}\n\teta: {prm.eta:3.3f}")
+
+
+def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16,
+                       verbose=False, plan=None):
+    """Doubly-periodic Stokeslet by spectral Ewald (StokesSLP_ewald_2p.m:1-138).
+
+    Returns (u1, u2, ur, uk, xi); ur and uk are 2 x Ntar like the MATLAB
+    outputs."""
+    xs, ys, xt, yt = map(_col, (xsrc, ysrc, xtar, ytar))
+    f = np.vstack([_col(f1), _col(f2)])
+    npts = xs.size + xt.size
+    if Nb is None:
+        Nb = min(P * _round_half_away(math.log2(npts)), npts / 4)
+    prm = select_params("slp", xs.size, xt.size, float(np.sum(f ** 2)), Lx, Ly, P, Nb, tol)
+    if verbose:
+        _verbose_print("slp", prm, xs.size, xt.size, tol, Nb)
+    u, ur, uk = slp_ewald(np.vstack([xs, ys]), np.vstack([xt, yt]), f, prm, parts=True,
+                          plan=plan)
+    return u[0], u[1], ur, uk, prm.xi
+
+
+def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=None,
+                       tol=1e-16, verbose=False, unit_normal_fix=True, plan=None):
+    """Doubly-periodic stresslet by spectral Ewald (StokesDLP_ewald_2p.m:1-365).
+
+    unit_normal_fix mirrors the driver's guard for MATLAB releases after
+    R2017a (StokesDLP_ewald_2p.m:69-80): n1 -= 1e-60, n2 = sqrt(1-n1^2) sign(n2),
+    f += 1e-60, i.e. normals are re-normalised from n1 and the sign of n2.
+    Returns (u1, u2, ur, uk, xi)."""
+    xs, ys, xt, yt = map(_col, (xsrc, ysrc, xtar, ytar))
+    n1, n2, f1, f2 = map(_col, (n1, n2, f1, f2))
+    if unit_normal_fix:
+        off = 1e-60
+        n1 = n1 - off
+        if np.all(n1 < -1):
+            n1 = n1 + 2 * off
+        n2 = np.sqrt(1 - n1 ** 2) * np.sign(n2)
+        f1 = f1 + off
+        f2 = f2 + off
+    f = np.vstack([f1, f2])
+    npts = xs.size + xt.size
+    if Nb is None:
+        Nb = min(P * _round_half_away(math.log2(npts)), npts / 4)
+    # the DLP driver recomputes npts as length(psrc)+length(ptar) (:309)
+    ns_len = max(xs.size, 2) if xs.size else 0
+    nt_len = max(xt.size, 2) if xt.size else 0
+    prm = select_params("dlp", ns_len, nt_len, float(np.sum(f ** 2)), Lx, Ly, P, Nb, tol)
+    if verbose:
+        _verbose_print("dlp", prm, xs.size, xt.size, tol, Nb)
+    u, ur, uk = dlp_ewald(np.vstack([xs, ys]), np.vstack([xt, yt]), f, np.vstack([n1, n2]), prm,
+                          parts=True, plan=plan)
+    return u[0], u[1], ur, uk, prm.xi

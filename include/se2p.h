@@ -1,0 +1,122 @@
+/*
+ * se2p.h -- C ABI of libse2p: doubly-periodic spectral Ewald (SE) summation of
+ * the 2D Stokeslet (single layer, SLP) and stresslet (double layer, DLP) on a
+ * GB300 GPU (sm_103a).
+ *
+ * Drop-in for the spectral-Ewald path of FastTools2D (PeriodicEwald):
+ *   - the four MEX gateways keep their argument order and meaning,
+ *   - the two driver composites reproduce the MATLAB drivers' post-processing
+ *     (wrap into [-L/2, L/2), real + k-space parts, DLP k=0 term, DLP sign)
+ *     for given Ewald parameters.
+ *
+ * Data layout is MATLAB's: a "2xN" array is N interleaved (x, y) doubles.
+ * Every array argument may be host memory (pageable or pinned) or device
+ * memory of the plan's device; the library stages host data itself.  With
+ * any host argument the call returns after the results are in host memory;
+ * with device-only arguments the work is queued on the plan's stream and the
+ * call returns without synchronising.
+ *
+ * Calls on one plan must not overlap; distinct plans are independent.
+ * Every function returns an se2p_status; se2p_plan_last_error() gives the
+ * message of the last failure on that plan.
+ */
+#ifndef SE2P_H
+#define SE2P_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SE2P_OK = 0,
+    SE2P_ERR_ARG = 1,          /* bad shape or parameter (the MEX gateways' mexErrMsgTxt cases) */
+    SE2P_ERR_CUDA = 2,         /* CUDA runtime failure */
+    SE2P_ERR_CUFFT = 3,        /* cuFFT failure */
+    SE2P_ERR_ALLOC = 4,        /* device allocation failure */
+    SE2P_ERR_UNSUPPORTED = 5   /* valid for the reference, outside this library's limits */
+} se2p_status;
+
+typedef struct se2p_plan_st *se2p_plan;
+
+/* Ewald parameters of one evaluation (the MEX-level arguments). */
+typedef struct {
+    double xi;            /* Ewald splitting parameter */
+    int nside_x, nside_y; /* real-space boxes per axis; cutoff^2 = Lx*Ly/nside_x/nside_y */
+    int Mx, My;           /* k-space grid, even, with Lx/Mx == Ly/My */
+    int P;                /* Gaussian support: P+1 nodes per axis, P even, P <= 30 */
+    double Lx, Ly;        /* periodic box */
+    double w;             /* Gaussian width P*h/2 (as passed by the drivers) */
+    double eta;           /* spectral splitting parameter */
+} se2p_params;
+
+/* ---- plans ---------------------------------------------------------------
+ * A plan owns a CUDA stream, reusable device workspace and cached cuFFT
+ * plans.  No reference counterpart (the MEX gateways allocate per call). */
+int se2p_plan_create(se2p_plan *plan, int device);
+int se2p_plan_destroy(se2p_plan plan);
+/* Queue the plan's work on an existing cudaStream_t; NULL selects CUDA's
+ * legacy default stream (as cublasSetStream / cufftSetStream do).  A new plan
+ * uses a private non-blocking stream. */
+int se2p_plan_set_stream(se2p_plan plan, void *cuda_stream);
+const char *se2p_plan_last_error(se2p_plan plan);
+/* Bytes of device workspace the plan currently holds. */
+int64_t se2p_plan_workspace_bytes(se2p_plan plan);
+/* Number of kernels this plan has launched so far (its own, not cuFFT's). */
+int64_t se2p_plan_kernel_launches(se2p_plan plan);
+const char *se2p_version(void);
+
+/* ---- MEX gateways ----------------------------------------------------------
+ * Replaces mex_stokes_slp_real(psrc, ptar, f, xi, nside_x, nside_y, Lx, Ly)
+ * (PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_real.cpp:58-83). */
+int se2p_slp_real(se2p_plan plan, const double *psrc, int64_t nsrc, const double *ptar,
+                  int64_t ntar, const double *f, double xi, int nside_x, int nside_y,
+                  double Lx, double Ly, double *u);
+
+/* Replaces mex_stokes_slp_kspace(psrc, ptar, xi, eta, f, Mx, My, Lx, Ly, w, P)
+ * (PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:8-42). */
+int se2p_slp_kspace(se2p_plan plan, const double *psrc, int64_t nsrc, const double *ptar,
+                    int64_t ntar, double xi, double eta, const double *f, int Mx, int My,
+                    double Lx, double Ly, double w, int P, double *u);
+
+/* Replaces mex_stokes_dlp_real(psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly)
+ * (PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:15-52). */
+int se2p_dlp_real(se2p_plan plan, const double *psrc, int64_t nsrc, const double *ptar,
+                  int64_t ntar, const double *f, const double *n, double xi, int nside_x,
+                  int nside_y, double Lx, double Ly, double *u);
+
+/* Replaces mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P)
+ * (PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_kspace.cpp:10-53). */
+int se2p_dlp_kspace(se2p_plan plan, const double *psrc, int64_t nsrc, const double *ptar,
+                    int64_t ntar, double xi, double eta, const double *f, const double *n,
+                    int Mx, int My, double Lx, double Ly, double w, int P, double *u);
+
+/* ---- driver composites -----------------------------------------------------
+ * The part of StokesSLP_ewald_2p.m after parameter selection
+ * (PeriodicEwald/src/matlab/StokesSLP_ewald_2p.m:74-82, :119-133):
+ * wrap points into [-L/2, L/2), u = ur + uk.  ur / uk may be NULL. */
+int se2p_slp_ewald(se2p_plan plan, const se2p_params *prm, const double *psrc, int64_t nsrc,
+                   const double *ptar, int64_t ntar, const double *f, double *u, double *ur,
+                   double *uk);
+
+/* StokesDLP_ewald_2p.m:295-360 after parameter selection: wrap, ur, uk,
+ * uk -= sum((f.n) x_src)/(Lx Ly) over the UNWRAPPED sources, u = -(ur + uk).
+ * ur / uk (may be NULL) receive the parts as the driver returns them. */
+int se2p_dlp_ewald(se2p_plan plan, const se2p_params *prm, const double *psrc, int64_t nsrc,
+                   const double *ptar, int64_t ntar, const double *f, const double *n,
+                   double *u, double *ur, double *uk);
+
+/* Both drivers on one point set in one pass: u_slp as se2p_slp_ewald with
+ * forces f_slp, u_dlp as se2p_dlp_ewald with density f_dlp and normals n.
+ * Sorting, Gaussian weights, cuFFT batches and the real-space walk are
+ * shared.  No single reference counterpart: it equals calling
+ * StokesSLP_ewald_2p.m and StokesDLP_ewald_2p.m with the same parameters. */
+int se2p_stokes_ewald(se2p_plan plan, const se2p_params *prm, const double *psrc,
+                      int64_t nsrc, const double *ptar, int64_t ntar, const double *f_slp,
+                      const double *f_dlp, const double *n, double *u_slp, double *u_dlp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SE2P_H */
