@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark: doubly-periodic spectral Ewald, 2D Stokeslet (SLP) + stresslet
+(DLP), FP64, N = 2^20 sources and targets, on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one SE evaluation of both potentials on the workload (sort, real
+space, spread, FFTs, filter, gather, DLP k=0 term) through se2p_stokes_ewald.
+
+Workload (xi=860, rc=0.0056 -> nside=178, M=2688, P=24, tolerance 1e-10):
+1,048,576 sources and 1,048,576 separate targets uniform in the unit box,
+SLP forces and DLP densities N(0,1), uniformly random unit normals, seed
+20261203+3.  Synthetic data: the reference names no dataset.
+
+Printed JSON line:
+  value         evals/s with inputs resident in HBM (whole job, all ranks)
+  e2e           evals/s through the C ABI with pinned HOST buffers, the
+                host->device copies of the inputs and device->host copies of
+                both outputs inside the timed region
+  roofline      dominant kernel: executed FP64 FLOP/s against the FP64 peak
+                measured in this run (cuBLAS DGEMM), plus its HBM side
+  cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP path)
+                on this host's cores, one full evaluation
+  gpu_launches  this library's kernel launches in the timed region
+  clocks        nvidia-smi samples taken during the timed region
+
+L2 (126 MB) is flushed between timed steps by writing a 256 MB buffer
+(outside the timed intervals); the evaluation's own working set is ~0.9 GB.
+
+With --impl reference the CPU reference path is timed instead (the
+reference's own sources built under oracle/_ref where they compile, else the
+oracle port), on all host threads, on the same workload; one step = one full
+evaluation.  Under torchrun only rank 0 runs it.
+
+Multi-GPU (torchrun, N > 1): independent replicas, one per GPU, no
+collective on the data path (weak scaling); the timed region is bracketed by
+barriers and the maximum time over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 2 ** 20
+XI, RC, M, P, L = 860.0, 0.0056, 2688, 24, 1.0
+SEED = 20261203 + 3
+METRIC = "SE Stokes evals/s @1M pts: FP64 tol 1e-10 vs FP32-grid tol 1e-6; fwd+adjoint time"
+UNIT = "evals/s"
+# FP64 FLOPs the fused real-space kernel executes per counted pair (SLP and
+# DLP pairs counted separately, candidate tests included): ncu sass counters
+# 2*DFMA + DMUL + DADD = 16.87 GFLOP over 219.8 M pairs on this workload
+# (profiles/k_real_cfg3.md).  Used only to express the kernel's time as FLOP/s.
+REAL_FP64_FLOP_PER_PAIR = 76.76
+# DRAM bytes (read + write) of one k_real launch on this workload, same capture.
+REAL_DRAM_BYTES = 188.4e6
+
+
+def workload(N):
+    rng = np.random.default_rng(SEED)
+    psrc = rng.random((N, 2))
+    ptar = rng.random((N, 2))
+    f = rng.standard_normal((N, 2))
+    g = rng.standard_normal((N, 2))
+    th = rng.random(N) * 2 * np.pi
+    n = np.stack([np.cos(th), np.sin(th)], axis=1)
+    return psrc, ptar, f, g, n
+
+
+def params(N):
+    import fasttools2d_gb300 as ft
+    nside = int(math.floor(L / RC))
+    return ft.EwaldParams.derived(XI, nside, nside, M, M, P, L, L)
+
+
+def config(N, extra=None):
+    c = {"workload": f"SE SLP+DLP FP64, N={N} sources + {N} targets uniform in L=1, "
+                     f"xi={XI}, rc={RC} (nside={int(L / RC)}), M={M}, P={P}, tol 1e-10",
+         "N_sources": N, "N_targets": N, "xi": XI, "rc": RC, "nside": int(L / RC), "M": M,
+         "P": P, "L": L, "l2": "flushed between timed steps (256 MB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_id), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return False
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return None
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU paths (oracle port / compiled reference), used for cpu_baseline and
+# the reference arm
+# ---------------------------------------------------------------------------
+def cpu_eval_fn(N, prefer_reference):
+    from oracle import oracle as O
+    psrc, ptar, f, g, n = workload(N)
+    prm = params(N)
+    S, T = psrc.T.copy(), ptar.T.copy()
+    F, G, Nn = f.T.copy(), g.T.copy(), n.T.copy()
+    kind = "port"
+    if prefer_reference:
+        from oracle import ref_mex
+        if ref_mex.available():
+            kind = "reference"
+            R = ref_mex.RefMex()
+
+            def run():
+                ps = np.vstack([O.wrap(S[0], L), O.wrap(S[1], L)])
+                pt = np.vstack([O.wrap(T[0], L), O.wrap(T[1], L)])
+                R.slp_real(ps, pt, F, prm.xi, prm.nside_x, prm.nside_y, L, L)
+                R.slp_kspace(ps, pt, prm.xi, prm.eta, F, M, M, L, L, prm.w, P)
+                R.dlp_real(ps, pt, G, Nn, prm.xi, prm.nside_x, prm.nside_y, L, L)
+                R.dlp_kspace(ps, pt, prm.xi, prm.eta, G, Nn, M, M, L, L, prm.w, P)
+                O.dlp_zero_mode(S, G, Nn, L, L)
+            return run, kind
+
+    def run():
+        O.slp_ewald(S, T, F, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)
+        O.dlp_ewald(S, T, G, Nn, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)
+    return run, kind
+
+
+def cpu_threads():
+    from oracle import oracle as O
+    return O.num_threads()
+
+
+def cpu_baseline(N):
+    run, kind = cpu_eval_fn(N, prefer_reference=False)
+    t0 = time.perf_counter()
+    run()
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": cpu_threads(), "kind": kind,
+            "sample": f"one full SLP+DLP evaluation at N={N} (oracle C restatement, OpenMP, "
+                      f"scipy FFT), {dt:.2f} s"}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    N = args.n
+    run, kind = cpu_eval_fn(N, prefer_reference=True)
+    for _ in range(args.warmup):
+        run()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        run()
+        ts.append(time.perf_counter() - t0)
+    total = sum(ts)
+    value = args.steps / total
+    cores = cpu_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config(N, {"parallelism": "cpu-openmp"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"full SLP+DLP evaluation at N={N} per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def fp64_peak_tflops(torch, dev):
+    """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
+    n = 2048
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = 1e30
+    for _ in range(5):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    import fasttools2d_gb300 as ft
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    N = args.n
+    prm = params(N)
+    psrc, ptar, f, g, n = workload(N)
+    tens = [torch.from_numpy(a).to(dev) for a in (psrc, ptar, f, g, n)]
+    plan = ft.Plan(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 2 ** 20, dtype=torch.float32, device=dev)   # 256 MB
+    cprm = prm.as_c()
+    L_ = plan.lib
+
+    u_dev = [torch.empty((N, 2), dtype=torch.float64, device=dev) for _ in range(2)]
+
+    def step_device():
+        plan.check(L_.se2p_stokes_ewald(plan.handle, ctypes.byref(cprm), tens[0].data_ptr(), N,
+                                        tens[1].data_ptr(), N, tens[2].data_ptr(),
+                                        tens[3].data_ptr(), tens[4].data_ptr(),
+                                        u_dev[0].data_ptr(), u_dev[1].data_ptr()))
+
+    pin = [torch.from_numpy(a).pin_memory() for a in (psrc, ptar, f, g, n)]
+    u_host = [torch.empty((N, 2), dtype=torch.float64).pin_memory() for _ in range(2)]
+
+    def step_host():
+        plan.check(L_.se2p_stokes_ewald(plan.handle, ctypes.byref(cprm), pin[0].data_ptr(), N,
+                                        pin[1].data_ptr(), N, pin[2].data_ptr(),
+                                        pin[3].data_ptr(), pin[4].data_ptr(),
+                                        u_host[0].data_ptr(), u_host[1].data_ptr()))
+
+    def timed(step, steps):
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            s = torch.cuda.Event(enable_timing=True)
+            e = torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            step()
+            e.record(stream)
+            ms.append((s, e))
+        torch.cuda.synchronize(dev)
+        return sum(s.elapsed_time(e) for s, e in ms)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize(dev)
+
+    # ---- device-resident timed region -------------------------------------
+    plan.enable_timing(True)
+    plan.stage_times(reset=True)
+    plan.count_pairs(True, reset=True)
+    launches0 = plan.kernel_launches
+    gpu_id = local_rank
+    try:
+        gpu_id = str(torch.cuda.get_device_properties(dev).uuid)
+        gpu_id = gpu_id if gpu_id.startswith("GPU-") else "GPU-" + gpu_id
+    except Exception:
+        pass
+    barrier()
+    with ClockSampler(gpu_id) as clk:
+        total_ms = timed(step_device, args.steps)
+        barrier()
+    launches = plan.kernel_launches - launches0
+    counts = plan.count_pairs(False, reset=True)
+    stages = plan.stage_times(reset=True)
+    plan.enable_timing(False)
+    total_ms = max_over_ranks(total_ms)
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers ------------
+    for _ in range(max(1, args.warmup // 2)):
+        step_host()
+    barrier()
+    e2e_ms = max_over_ranks(timed(step_host, args.steps))
+    barrier()
+    e2e = {"value": world * args.steps / (e2e_ms * 1e-3), "unit": UNIT,
+           "h2d_bytes_per_step": 5 * N * 16, "d2h_bytes_per_step": 2 * N * 16,
+           "ms_per_step": e2e_ms / args.steps}
+
+    # ---- roofline of the dominant kernel ---------------------------------
+    kstages = {k: v for k, v in stages.items() if k not in ("h2d", "d2h") and v[1] > 0}
+    top = max(kstages, key=lambda k: kstages[k][0])
+    top_ms = kstages[top][0] / kstages[top][1]
+    peak = fp64_peak_tflops(torch, dev)
+    pairs_per_launch = (counts[1] + counts[2]) / max(1, kstages.get("real", (0, 1))[1])
+    real_ms = kstages["real"][0] / kstages["real"][1] if "real" in kstages else float("nan")
+    real_flops = pairs_per_launch * REAL_FP64_FLOP_PER_PAIR
+    roof = {"kernel": "k_real (fused SLP+DLP real-space pair sum)", "bound": "fp64",
+            "achieved": real_flops / (real_ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "peak_source": "cuBLAS DGEMM 2048^3 measured in this run "
+                           "(MEASURED_PEAKS.json holds no FP64 figure)",
+            "traffic": REAL_DRAM_BYTES, "traffic_unit": "bytes/launch (ncu)",
+            "ms_per_launch": real_ms,
+            "accepted_pairs_per_launch": pairs_per_launch,
+            "candidates_per_launch": counts[0] / max(1, kstages.get("real", (0, 1))[1]),
+            "pairs_per_s": pairs_per_launch / (real_ms * 1e-3),
+            "flop_per_pair": REAL_FP64_FLOP_PER_PAIR, "top_stage": top,
+            "top_stage_ms": top_ms}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1] > 0}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config(N, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+        "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(N)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT, help="points (sources = targets count)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    gpu_arm(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -23,6 +23,8 @@ EXPORTS = (
     "se2p_plan_last_error", "se2p_plan_workspace_bytes", "se2p_plan_kernel_launches",
     "se2p_slp_real", "se2p_slp_kspace", "se2p_dlp_real", "se2p_dlp_kspace",
     "se2p_slp_ewald", "se2p_dlp_ewald", "se2p_stokes_ewald",
+    "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
+    "se2p_plan_count_pairs",
 )
 
 
@@ -71,6 +73,12 @@ def load(path: str = LIB_PATH):
         L.se2p_dlp_real.argtypes = [P, _dp, i64, _dp, i64, _dp, _dp, d, i32, i32, d, d, _dp]
         L.se2p_dlp_kspace.argtypes = [P, _dp, i64, _dp, i64, d, d, _dp, _dp, i32, i32, d, d, d,
                                       i32, _dp]
+        L.se2p_plan_enable_timing.argtypes = [P, i32]
+        L.se2p_stage_name.argtypes = [i32]
+        L.se2p_stage_name.restype = ctypes.c_char_p
+        L.se2p_plan_stage_times.argtypes = [P, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_int64), i32]
+        L.se2p_plan_count_pairs.argtypes = [P, i32, ctypes.POINTER(ctypes.c_int64), i32]
         PP = ctypes.POINTER(Params)
         L.se2p_slp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp]
         L.se2p_dlp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp]
@@ -107,6 +115,24 @@ class Plan:
     @property
     def kernel_launches(self) -> int:
         return self.lib.se2p_plan_kernel_launches(self.handle)
+
+    def enable_timing(self, on: bool = True):
+        self.check(self.lib.se2p_plan_enable_timing(self.handle, 1 if on else 0))
+
+    def stage_times(self, reset: bool = True):
+        """{stage: (total_ms, calls)} accumulated since the last reset."""
+        n = self.lib.se2p_num_stages()
+        ms = (ctypes.c_double * n)()
+        calls = (ctypes.c_int64 * n)()
+        self.check(self.lib.se2p_plan_stage_times(self.handle, ms, calls, 1 if reset else 0))
+        return {self.lib.se2p_stage_name(i).decode(): (ms[i], calls[i]) for i in range(n)}
+
+    def count_pairs(self, on: bool = True, reset: bool = True):
+        """Turn the real-space counters on/off; returns (candidates, slp_pairs, dlp_pairs)."""
+        c = (ctypes.c_int64 * 3)()
+        self.check(self.lib.se2p_plan_count_pairs(self.handle, 1 if on else 0, c,
+                                                  1 if reset else 0))
+        return tuple(c)
 
     def close(self):
         if self.handle:

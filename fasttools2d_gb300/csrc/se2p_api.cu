@@ -31,9 +31,9 @@ enum Slot {
     S_WPS, S_WPT,                               // wrapped positions
     S_SBOX, S_SRANK, S_TBOX, S_TRANK, S_COUNT,  // binning scratch
     S_SSTART, S_TSTART, S_SPERM, S_TPERM, S_TBOXS,
-    S_SP, S_TP, S_COEF,                         // sorted data
+    S_SP, S_TP, S_SPF, S_TPF, S_COEF,           // sorted data
     S_UR_SLP, S_UR_DLP, S_UK,                   // partial results (sorted order)
-    S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM,
+    S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM, S_COUNTERS,
     S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
     S_COUNT_SLOTS
 };
@@ -45,6 +45,15 @@ struct DevBuf {
 
 }  // namespace
 
+// Stages timed with CUDA events when timing is on (se2p_plan_enable_timing).
+enum Stage {
+    T_STAGE_IN, T_WRAP, T_SORT, T_COEF, T_REAL, T_SPREAD, T_FFT_FWD, T_FILTER, T_FFT_INV,
+    T_GATHER, T_ZERO_MODE, T_ASSEMBLE, T_STAGE_OUT, T_NUM_STAGES
+};
+static const char *kStageNames[T_NUM_STAGES] = {
+    "h2d", "wrap", "sort", "coef", "real", "spread", "fft_fwd", "filter", "fft_inv",
+    "gather", "zero_mode", "assemble", "d2h"};
+
 struct se2p_plan_st {
     int device = 0;
     cudaStream_t own = nullptr;
@@ -53,6 +62,12 @@ struct se2p_plan_st {
     int64_t launches = 0;
     DevBuf buf[S_COUNT_SLOTS];
     std::map<std::tuple<int, int, int, int>, cufftHandle> ffts;  // (Mx, My, batch, dir)
+    bool timing = false;
+    bool count_pairs = false;
+    // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NUM_STAGES];
+    double stage_ms[T_NUM_STAGES] = {0};
+    int64_t stage_calls[T_NUM_STAGES] = {0};
 };
 
 namespace {
@@ -86,6 +101,29 @@ int fail(se2p_plan pl, int code, const char *fmt, ...)
         int s_ = (call);                \
         if (s_ != SE2P_OK) return s_;   \
     } while (0)
+
+// Brackets one stage of one call with events on the plan's stream.
+struct StageTimer {
+    se2p_plan pl;
+    int stage;
+    cudaEvent_t a = nullptr, b = nullptr;
+    StageTimer(se2p_plan p, int st) : pl(p), stage(st)
+    {
+        if (!pl->timing) return;
+        if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+            cudaGetLastError();
+            a = b = nullptr;
+            return;
+        }
+        cudaEventRecord(a, pl->stream);
+    }
+    ~StageTimer()
+    {
+        if (!a) return;
+        cudaEventRecord(b, pl->stream);
+        pl->pending[stage].emplace_back(a, b);
+    }
+};
 
 struct DeviceGuard {
     int prev = -1;
@@ -294,6 +332,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     const int64_t ns = io.ns, nt = io.nt;
 
     const double2 *ps = nullptr, *pt = nullptr, *fs = nullptr, *fd = nullptr, *nr = nullptr;
+    StageTimer *t_in = new StageTimer(pl, T_STAGE_IN);
     CKS(stage_in(pl, S_IN_PS, io.psrc, ns, &ps, &host_io));
     CKS(stage_in(pl, S_IN_PT, io.ptar, nt, &pt, &host_io));
     if (J.slp) CKS(stage_in(pl, S_IN_F, io.f_slp, ns, &fs, &host_io));
@@ -307,6 +346,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     // Parts are rarely requested; they share two extra slots per kind.
     CKS(stage_out(pl, S_OUT2, io.ur_slp ? io.ur_slp : io.ur_dlp, nt, io.ur_slp ? &o_urs : &o_urd, &host_io));
     CKS(stage_out(pl, S_OUT3, io.uk_slp ? io.uk_slp : io.uk_dlp, nt, io.uk_slp ? &o_uks : &o_ukd, &host_io));
+    delete t_in;
     if (io.ur_slp && io.ur_dlp) return fail(pl, SE2P_ERR_ARG, "internal: both part outputs requested");
 
     if (nt == 0) return SE2P_OK;
@@ -314,6 +354,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     // Wrapped positions (driver composites); the raw sources stay for the zero mode.
     const double2 *ws = ps, *wt = pt;
     if (J.wrap) {
+        StageTimer tm(pl, T_WRAP);
         double2 *a = nullptr, *b = nullptr;
         if (ns > 0) {
             CKS(ensure_t(pl, S_WPS, (size_t)ns, &a));
@@ -349,17 +390,28 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     CKS(ensure_t(pl, S_SP, nsz, &sp));
     CKS(ensure_t(pl, S_TP, ntz, &tp));
 
+    float2 *spf = nullptr, *tpf = nullptr;
+    if (J.real) {
+        CKS(ensure_t(pl, S_SPF, nsz, &spf));
+        CKS(ensure_t(pl, S_TPF, ntz, &tpf));
+    }
+    {
+    StageTimer tm(pl, T_SORT);
     BinArgs bs{ws, ns, J.Lx, J.Ly, nx, ny, sbox, srank, count};
-    CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, st, pl->launches));
+    CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, spf, st, pl->launches));
     BinArgs bt{wt, nt, J.Lx, J.Ly, nx, ny, tbox, trank, count};
-    CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, st, pl->launches));
+    CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, tpf, st, pl->launches));
+    }
 
     const int nc = (J.slp ? 2 : 0) + (J.dlp ? 3 : 0);
     const int doff = J.slp ? 2 : 0;
     double *coef = nullptr;
     CKS(ensure_t(pl, S_COEF, (size_t)nc * nsz, &coef));
-    CK(launch_src_coef(ns, sperm, J.slp ? fs : nullptr, J.dlp ? fd : nullptr, nr, coef, nc, st,
-                       pl->launches));
+    {
+        StageTimer tm(pl, T_COEF);
+        CK(launch_src_coef(ns, sperm, J.slp ? fs : nullptr, J.dlp ? fd : nullptr, nr, coef, nc, st,
+                           pl->launches));
+    }
 
     double2 *ur_slp = nullptr, *ur_dlp = nullptr, *uk = nullptr;
     if (J.real) {
@@ -367,6 +419,8 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         if (J.dlp) CKS(ensure_t(pl, S_UR_DLP, ntz, &ur_dlp));
         RealArgs ra;
         ra.sp = sp;
+        ra.spf = spf;
+        ra.tpf = tpf;
         ra.coef = coef;
         ra.nc = nc;
         ra.doff = doff;
@@ -381,9 +435,28 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ra.xi = J.xi;
         ra.xi2 = J.xi * J.xi;
         ra.cut2 = J.Lx * J.Ly / nx / ny;                 // mex_stokes_slp_real.cpp:127
+        ra.cut2f = (float)ra.cut2;
+        ra.inv_xi2 = 1.0 / (J.xi * J.xi);
+        ra.pf = 2.0 * J.xi * J.xi;
+        // (len*(per_source - t))/nside with per_source - t = -+nside
+        // (mex_stokes_slp_real.cpp:248-249)
+        ra.zxm = (J.Lx * (double)(-nx)) / nx;
+        ra.zxp = (J.Lx * (double)nx) / nx;
+        ra.zym = (J.Ly * (double)(-ny)) / ny;
+        ra.zyp = (J.Ly * (double)ny) / ny;
         ra.self_c = -1.288607832450766155 - std::log(J.xi);  // mex_stokes_slp_real.cpp:124
         ra.u_slp = ur_slp;
         ra.u_dlp = ur_dlp;
+        ra.counters = nullptr;
+        if (pl->count_pairs) {
+            if (!pl->buf[S_COUNTERS].p) {
+                unsigned long long *c = nullptr;
+                CKS(ensure_t(pl, S_COUNTERS, 3, &c));
+                CK(cudaMemsetAsync(c, 0, 3 * sizeof(unsigned long long), st));
+            }
+            ra.counters = static_cast<unsigned long long *>(pl->buf[S_COUNTERS].p);
+        }
+        StageTimer tm(pl, T_REAL);
         CK(launch_real(ra, J.slp, J.dlp, st, pl->launches));
     }
 
@@ -419,11 +492,17 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         sa.w = J.w;
         sa.a = -2 * J.xi * J.xi / J.eta;
         sa.e1 = e1;
-        CK(launch_spread(sa, nc, st, pl->launches));
+        {
+            StageTimer tm(pl, T_SPREAD);
+            CK(launch_spread(sa, nc, st, pl->launches));
+        }
 
         cufftHandle fwd, inv;
         CKS(get_fft(pl, Mx, My, nc, 0, &fwd));
-        CKF(cufftExecD2Z(fwd, grid, spec));
+        {
+            StageTimer tm(pl, T_FFT_FWD);
+            CKF(cufftExecD2Z(fwd, grid, spec));
+        }
 
         FilterArgs fa;
         fa.spec = spec;
@@ -438,10 +517,16 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.dlp_in = J.dlp ? doff : -1;
         fa.slp_out = 0;
         fa.dlp_out = J.slp ? 2 : 0;
-        CK(launch_filter(fa, st, pl->launches));
+        {
+            StageTimer tm(pl, T_FILTER);
+            CK(launch_filter(fa, st, pl->launches));
+        }
 
         CKS(get_fft(pl, Mx, My, nout, 1, &inv));
-        CKF(cufftExecZ2D(inv, spec, grid));
+        {
+            StageTimer tm(pl, T_FFT_INV);
+            CKF(cufftExecZ2D(inv, spec, grid));
+        }
 
         GatherArgs ga;
         ga.tp = tp;
@@ -460,6 +545,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ga.scale = s / (4 * kPi);
         ga.e1 = e1;
         ga.out = uk;
+        StageTimer tm(pl, T_GATHER);
         CK(launch_gather(ga, nout, st, pl->launches));
     }
 
@@ -469,9 +555,11 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
         CKS(ensure_t(pl, S_ZM, 1, &zm));
         // sum over the caller's (unwrapped) sources
+        StageTimer tm(pl, T_ZERO_MODE);
         CK(launch_zero_mode(ns, ps, fd, nr, 1.0 / (J.Lx * J.Ly), part, zm, st, pl->launches));
     }
 
+    StageTimer *t_asm = new StageTimer(pl, T_ASSEMBLE);
     const double2 *uk_slp = (J.kspace && J.slp) ? uk : nullptr;
     const double2 *uk_dlp = (J.kspace && J.dlp) ? uk + (J.slp ? nt : 0) : nullptr;
     if (J.slp && o_us.dev)
@@ -481,12 +569,15 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         CK(launch_assemble(nt, io.mode_dlp, tperm, J.real ? ur_dlp : nullptr, uk_dlp, zm,
                            o_ud.dev, o_urd.dev, o_ukd.dev, st, pl->launches));
 
+    delete t_asm;
+    StageTimer *t_out = new StageTimer(pl, T_STAGE_OUT);
     CKS(finish_out(pl, o_us));
     CKS(finish_out(pl, o_ud));
     CKS(finish_out(pl, o_urs));
     CKS(finish_out(pl, o_urd));
     CKS(finish_out(pl, o_uks));
     CKS(finish_out(pl, o_ukd));
+    delete t_out;
     if (host_io) CK(cudaStreamSynchronize(st));
     else CK(cudaGetLastError());
     return SE2P_OK;
@@ -528,6 +619,11 @@ int se2p_plan_destroy(se2p_plan pl)
     if (!pl) return SE2P_OK;
     DeviceGuard guard(pl->device);
     cudaStreamSynchronize(pl->stream);
+    for (auto &v : pl->pending)
+        for (auto &ev : v) {
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
     for (auto &kv : pl->ffts) cufftDestroy(kv.second);
     for (auto &b : pl->buf)
         if (b.p) cudaFree(b.p);
@@ -554,6 +650,62 @@ int64_t se2p_plan_workspace_bytes(se2p_plan pl)
 }
 
 int64_t se2p_plan_kernel_launches(se2p_plan pl) { return pl ? pl->launches : 0; }
+
+int se2p_plan_enable_timing(se2p_plan pl, int on)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    pl->timing = on != 0;
+    return SE2P_OK;
+}
+
+int se2p_num_stages(void) { return T_NUM_STAGES; }
+
+int se2p_plan_count_pairs(se2p_plan pl, int on, int64_t *counts, int reset)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    DeviceGuard guard(pl->device);
+    unsigned long long h[3] = {0, 0, 0};
+    void *c = pl->buf[S_COUNTERS].p;
+    if (c) {
+        CK(cudaStreamSynchronize(pl->stream));
+        CK(cudaMemcpy(h, c, sizeof h, cudaMemcpyDeviceToHost));
+        if (reset) CK(cudaMemset(c, 0, sizeof h));
+    }
+    if (counts)
+        for (int i = 0; i < 3; i++) counts[i] = (int64_t)h[i];
+    pl->count_pairs = on != 0;
+    return SE2P_OK;
+}
+
+const char *se2p_stage_name(int i) { return (i >= 0 && i < T_NUM_STAGES) ? kStageNames[i] : ""; }
+
+int se2p_plan_stage_times(se2p_plan pl, double *ms, int64_t *calls, int reset)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    DeviceGuard guard(pl->device);
+    for (int i = 0; i < T_NUM_STAGES; i++) {
+        for (auto &ev : pl->pending[i]) {
+            float t = 0.f;
+            if (cudaEventSynchronize(ev.second) == cudaSuccess &&
+                cudaEventElapsedTime(&t, ev.first, ev.second) == cudaSuccess) {
+                pl->stage_ms[i] += t;
+                pl->stage_calls[i]++;
+            } else {
+                cudaGetLastError();
+            }
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
+        pl->pending[i].clear();
+        if (ms) ms[i] = pl->stage_ms[i];
+        if (calls) calls[i] = pl->stage_calls[i];
+        if (reset) {
+            pl->stage_ms[i] = 0;
+            pl->stage_calls[i] = 0;
+        }
+    }
+    return SE2P_OK;
+}
 
 int se2p_slp_real(se2p_plan pl, const double *psrc, int64_t ns, const double *ptar, int64_t nt,
                   const double *f, double xi, int nside_x, int nside_y, double Lx, double Ly,

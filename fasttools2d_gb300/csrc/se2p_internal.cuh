@@ -129,17 +129,23 @@ struct BinArgs {
 
 struct RealArgs {
     const double2 *sp;    // sources, sorted by box
+    const float2 *spf;    // the same rounded to FP32 (cutoff pre-test)
     const double *coef;   // nc coefficients per sorted source: SLP f at [0,1],
                           // DLP S = f (x) n as (S11, S12+S21, S22) at [doff, doff+3)
     int nc, doff;
     const int *sstart;    // box b's sources: [sstart[b], sstart[b+1])
     const double2 *tp;    // targets, sorted by box
+    const float2 *tpf;
     const int *tbox;      // box of each sorted target
     int64_t ntar;
     int nx, ny;
     double Lx, Ly, xi, xi2, cut2, self_c;
+    double inv_xi2, pf;   // 1/xi^2, 2 xi^2
+    double zxm, zxp, zym, zyp;   // image shifts (L*(-+nside))/nside of the wrapped neighbours
+    float cut2f;
     double2 *u_slp;       // raw sums per sorted target (no 1/(4 pi))
     double2 *u_dlp;
+    unsigned long long *counters;   // [candidates, SLP pairs, DLP pairs] (may be NULL)
 };
 
 struct SpreadArgs {
@@ -174,7 +180,8 @@ struct GatherArgs {
 // Host launchers (se2p_kernels.cu).  Each returns the launch status.
 // ---------------------------------------------------------------------------
 cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *sorted_box,
-                       double2 *sorted_pos, cudaStream_t st, int64_t &launches);
+                       double2 *sorted_pos, float2 *sorted_pos_f, cudaStream_t st,
+                       int64_t &launches);
 cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
                             const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
                             cudaStream_t st, int64_t &launches);

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, in
 __global__ void k_bin_place(int64_t n, const int *__restrict__ box, const int *__restrict__ rank,
                             const int *__restrict__ start, int *__restrict__ perm,
                             int *__restrict__ sorted_box, const double2 *__restrict__ p,
-                            double2 *__restrict__ sp)
+                            double2 *__restrict__ sp, float2 *__restrict__ spf)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -90,7 +90,9 @@ __global__ void k_bin_place(int64_t n, const int *__restrict__ box, const int *_
     const int j = start[b] + rank[i];
     perm[j] = (int)i;
     if (sorted_box) sorted_box[j] = b;
-    sp[j] = p[i];
+    const double2 q = p[i];
+    sp[j] = q;
+    if (spf) spf[j] = make_float2((float)q.x, (float)q.y);
 }
 
 // Per-source coefficients in sorted order, nc per source: SLP f (f1, f2),
@@ -122,114 +124,405 @@ __global__ void k_src_coef(int64_t n, const int *__restrict__ perm,
 
 // ===========================================================================
 // Real-space pair sums (PE/src/mex/StokesSLP/mex_stokes_slp_real.cpp:131-333,
-// PE/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:103-187), fused.
+// PE/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:103-187), SLP and DLP fused.
 //
-// One warp per target.  The warp walks the target's own box (every pair, no
-// cutoff) and its 8 periodic neighbour boxes (pairs with r2 < cut2), 32
-// candidate sources at a time.  Candidates are tested with the reference's
-// exact arithmetic and the accepted ones are compacted into a per-warp queue;
-// whenever 32 are queued, each lane evaluates one pair.  The SLP and DLP
-// tests are separate because the reference forms the offsets in different
-// orders (SLP s-(t-z), DLP (s-t)+z); flag bit 0 = SLP pair, bit 1 = DLP pair.
+// One warp walks a sequence of targets.  For each target the candidate
+// sources of its own box (every pair, no cutoff) and its 8 periodic
+// neighbour boxes (pairs with r2 < Lx*Ly/nside_x/nside_y) form one list,
+// scanned 32 at a time.  The cutoff test runs in FP32 with a rigorous
+// rounding-error band; only candidates inside the band take the reference's
+// exact FP64 test, separately for the SLP offset s-(t-z) and the DLP offset
+// (s-t)+z.  Accepted pairs go into a per-warp FIFO that carries over from one
+// target to the next, so the FP64 pair evaluation always runs on 32 lanes.
+// Each lane keeps register sums tagged with the target they belong to; when
+// its next pair is for a later target, the lanes flush with a segmented
+// warp reduction into a small ring of per-target accumulators, and a target
+// is written out once every lane has moved past it.
+//
+// Per pair the SLP and DLP share one exp(-xi^2 r^2) (table-driven, Tang's
+// method) and one reciprocal 1/r2 (rcp.approx + Newton).  E1 uses the
+// reference's three Pade forms through one Horner loop whose coefficient
+// set is chosen per lane (shorter forms padded with leading zeros, which
+// leaves their values unchanged), so only the log of the near form diverges.
+// The DLP contraction is regrouped as fb x_i (x.S.x) + 2 xi^2 (...),
+// algebraically equal to the reference's T_ijk S_jk.
 // ===========================================================================
 constexpr int kRealWarps = 8;
+constexpr int kRing = 32;     // targets in flight per warp
 __constant__ int c_nb_dx[9] = {0, -1, -1, -1, 0, 0, 1, 1, 1};
 __constant__ int c_nb_dy[9] = {0, -1, 0, 1, -1, 1, -1, 0, 1};
 
-template <bool SLP, bool DLP>
-__device__ __forceinline__ void real_pair(const RealArgs &a, int s, int k, int fl, double2 T,
-                                          double2 z, double &s1, double &s2, double &d1,
-                                          double &d2)
+// 2^(-j/64), j = 0..63, correctly rounded.
+__constant__ double c_exp_tab[64] = {
+    0x1.0000000000000p+0,
+    0x1.fa7c1819e90d8p-1,
+    0x1.f50765b6e4540p-1,
+    0x1.efa1bee615a27p-1,
+    0x1.ea4afa2a490dap-1,
+    0x1.e502ee78b3ff6p-1,
+    0x1.dfc97337b9b5fp-1,
+    0x1.da9e603db3285p-1,
+    0x1.d5818dcfba487p-1,
+    0x1.d072d4a07897cp-1,
+    0x1.cb720dcef9069p-1,
+    0x1.c67f12e57d14bp-1,
+    0x1.c199bdd85529cp-1,
+    0x1.bcc1e904bc1d2p-1,
+    0x1.b7f76f2fb5e47p-1,
+    0x1.b33a2b84f15fbp-1,
+    0x1.ae89f995ad3adp-1,
+    0x1.a9e6b5579fdbfp-1,
+    0x1.a5503b23e255dp-1,
+    0x1.a0c667b5de565p-1,
+    0x1.9c49182a3f090p-1,
+    0x1.97d829fde4e50p-1,
+    0x1.93737b0cdc5e5p-1,
+    0x1.8f1ae99157736p-1,
+    0x1.8ace5422aa0dbp-1,
+    0x1.868d99b4492edp-1,
+    0x1.82589994cce13p-1,
+    0x1.7e2f336cf4e62p-1,
+    0x1.7a11473eb0187p-1,
+    0x1.75feb564267c9p-1,
+    0x1.71f75e8ec5f74p-1,
+    0x1.6dfb23c651a2fp-1,
+    0x1.6a09e667f3bcdp-1,
+    0x1.6623882552225p-1,
+    0x1.6247eb03a5585p-1,
+    0x1.5e76f15ad2148p-1,
+    0x1.5ab07dd485429p-1,
+    0x1.56f4736b527dap-1,
+    0x1.5342b569d4f82p-1,
+    0x1.4f9b2769d2ca7p-1,
+    0x1.4bfdad5362a27p-1,
+    0x1.486a2b5c13cd0p-1,
+    0x1.44e086061892dp-1,
+    0x1.4160a21f72e2ap-1,
+    0x1.3dea64c123422p-1,
+    0x1.3a7db34e59ff7p-1,
+    0x1.371a7373aa9cbp-1,
+    0x1.33c08b26416ffp-1,
+    0x1.306fe0a31b715p-1,
+    0x1.2d285a6e4030bp-1,
+    0x1.29e9df51fdee1p-1,
+    0x1.26b4565e27cddp-1,
+    0x1.2387a6e756238p-1,
+    0x1.2063b88628cd6p-1,
+    0x1.1d4873168b9aap-1,
+    0x1.1a35beb6fcb75p-1,
+    0x1.172b83c7d517bp-1,
+    0x1.1429aaea92de0p-1,
+    0x1.11301d0125b51p-1,
+    0x1.0e3ec32d3d1a2p-1,
+    0x1.0b5586cf9890fp-1,
+    0x1.0874518759bc8p-1,
+    0x1.059b0d3158574p-1,
+    0x1.02c9a3e778061p-1};
+
+// E1 Pade sets as (numerator, denominator) pairs, 11 pairs each, highest
+// power first: 0 = far (x >= 16, in 1/x), 1 = mid (1 < x < 16, in 1/x),
+// 2 = near (x <= 1, in x); far and near are padded with leading zeros.
+__constant__ double c_e1[3][22] = {
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+     -17.70313744792479226930481672752649, -2.03222164752550948918496942496859,
+     -9.56230625623594754358691716333851, 24.24775264986217493401454703416675,
+     -0.99999982131078080094255255971802, 34.82867640350680460414878325536847,
+     -0.00000000083503088648841284312372, 11.56228921223568129050818242831156},
+    {-1185.45720315201027667, -0.776491285282330997549,
+     -14751.4895786128450662, 1229.20784182403048905,
+     -54844.4587226402067411, 18455.4124737722049515,
+     -86273.1567711649528784, 86722.3403467334749201,
+     -66598.2652345418633509, 180329.498380501819718,
+     -27182.6254466733970467, 192104.047790227984431,
+     -6046.8250112711035463, 113057.05869159631492,
+     -724.581482791462469795, 38129.5594484818471461,
+     -43.3058660811817946037, 7417.37624454689546708,
+     -0.999999999999998811143, 809.193214954550328455,
+     -0.121013190657725568138e-18, 45.3058660811801465927},
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+     -0.000111507792921197858394, -0.528611029520217142048e-6,
+     -0.00399167106081113256961, 0.000131049900798434683324,
+     -0.0368031736257943745142, 0.00427347600017103698101,
+     -0.245088216639761496153, 0.056770677104207528384,
+     0.0320913665303559189999, 0.37091387659397013215,
+     0.0865197248079397976498, 1.0}};
+
+// exp(-x) for x >= 0 by Tang's table-driven method (P. T. P. Tang, "Table-
+// driven implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2), 1989): x = (n/64) ln 2 + r, |r| <= ln2/128,
+// exp(-x) = 2^-(n>>6) * 2^-((n&63)/64) * exp(-r) with a degree-5 Taylor
+// polynomial (truncation < 4e-17).  ln2/64 is split Cody-Waite style (36-bit
+// head).  Returns 0 beyond x = 700 and propagates NaN.
+__device__ __forceinline__ double exp_neg(double x, const double *tab)
 {
-    const double2 S = a.sp[s];
-    if (SLP && (fl & 1)) {
-        double dx, dy;
-        if (k == 0) {
-            dx = xsub(T.x, S.x);
-            dy = xsub(T.y, S.y);
-        } else {
-            dx = xsub(S.x, xsub(T.x, z.x));
-            dy = xsub(S.y, xsub(T.y, z.y));
+    const double kShift = 6755399441055744.0;   // 1.5 * 2^52
+    const double t = fma(x, 0x1.71547652b82fep+6, kShift);
+    const int n = __double2loint(t);
+    const double kd = t - kShift;
+    double r = fma(-kd, 0x1.62e42fefa0000p-7, x);
+    r = fma(-kd, 0x1.cf79abc9e3b3ap-46, r);
+    double p = fma(-r, 1.0 / 120.0, 1.0 / 24.0);
+    p = fma(-r, p, 1.0 / 6.0);
+    p = fma(-r, p, 0.5);
+    p = fma(-r, p, 1.0);
+    p = fma(-r, p, 1.0);
+    const double scale = __hiloint2double((1023 - (n >> 6)) << 20, 0);
+    const double v = p * tab[n & 63] * scale;
+    return x <= 700.0 ? v : (x == x ? 0.0 : x);
+}
+
+// 1/a by the hardware approximation plus two Newton-Raphson steps
+// (r <- r + r (1 - a r)); each step doubles the correct bits.
+__device__ __forceinline__ double rcp_nr(double a)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a));
+    double e = fma(-a, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-a, r, 1.0);
+    return fma(r, e, r);
+}
+
+struct RealWarp {
+    int2 q[64];                 // (sorted source, slot | k << 8 | flags << 12)
+    double acc[kRing][4];       // per-target sums: SLP u1, u2, DLP u1, u2
+    double2 tpos[kRing];
+    int tbox[kRing];
+    long long tidx[kRing];
+    long long tend[kRing];      // queue position after the target's last pair
+    int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
+    double2 nbz[9];
+    float2 nbzf[9];
+};
+
+// Segmented warp reduction of (v0..v3) by nondecreasing key; the last lane
+// of each segment with key >= 0 adds its sum into the ring slot key % kRing.
+__device__ __forceinline__ void seg_flush(RealWarp &W, int lane, int key, double v0, double v1,
+                                          double v2, double v3)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ko = __shfl_up_sync(~0u, key, o);
+        const double a0 = __shfl_up_sync(~0u, v0, o), a1 = __shfl_up_sync(~0u, v1, o);
+        const double a2 = __shfl_up_sync(~0u, v2, o), a3 = __shfl_up_sync(~0u, v3, o);
+        if (lane >= o && ko == key) {
+            v0 += a0; v1 += a1; v2 += a2; v3 += a3;
         }
-        const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
-        const double x = xmul(xmul(r2, a.xi), a.xi);
-        const double e = exp(-x);
-        const double E = e1_pade(x, e);
+    }
+    const int kn = __shfl_down_sync(~0u, key, 1);
+    if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
+        double *a = W.acc[key % kRing];
+        a[0] += v0; a[1] += v1; a[2] += v2; a[3] += v3;
+    }
+    __syncwarp();
+}
+
+template <bool SLP, bool DLP>
+__device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, int2 e,
+                                          const double *tab, const double *e1s, double &s1,
+                                          double &s2, double &d1, double &d2)
+{
+    const int s = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
+    const double2 S = a.sp[s];
+    const double2 T = W.tpos[slot];
+    // image shift of neighbour k: 0 or the reference's (L*(+-nside))/nside
+    const int tb = W.tbox[slot];
+    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    const double x1 = (S.x - T.x) + zx, x2 = (S.y - T.y) + zy;          // DLP form
+    const double dxs = S.x - (T.x - zx), dys = S.y - (T.y - zy);        // SLP form
+    // The two forms round identically except, rarely, across a periodic
+    // image (z != 0); each kernel then keeps its own r2 as the reference does.
+    const double r2 = fma(dxs, dxs, dys * dys);
+    const double x = r2 * a.xi2;
+    const double ex = exp_neg(x, tab);
+    const double ir2 = rcp_nr(r2);
+    // E1 (unified Horner over the three Pade forms)
+    const int set = x >= 16.0 ? 0 : (x > 1.0 ? 1 : 2);
+    const double *c = e1s + 22 * set;
+    const double z = set == 2 ? x : ir2 * a.inv_xi2;
+    double pa = c[0], pb = c[1];
+#pragma unroll
+    for (int i = 2; i < 22; i += 2) {
+        pa = fma(z, pa, c[i]);
+        pb = fma(z, pb, c[i + 1]);
+    }
+    const double den = set == 2 ? pb : pb + x;
+    const double qv = pa * rcp_nr(den);
+    double E;
+    if (set == 2) E = qv + x - log(x) - 0.66373538970947265625;
+    else E = ex * (z + qv);
+    if (SLP && (fl & 1)) {
         const double f1 = a.coef[(int64_t)a.nc * s], f2 = a.coef[(int64_t)a.nc * s + 1];
-        const double g = e / r2;
-        const double q = dx * f2 - dy * f1;
-        s1 += 0.5 * E * f1 + g * dy * q;
-        s2 += 0.5 * E * f2 - g * dx * q;
+        const double h = 0.5 * E, g = ex * ir2;
+        const double gq = g * fma(dxs, f2, -dys * f1);
+        s1 = fma(h, f1, fma(gq, dys, s1));
+        s2 = fma(h, f2, fma(-gq, dxs, s2));
     }
     if (DLP && (fl & 2)) {
-        double x1, x2;
-        if (k == 0) {
-            x1 = xsub(S.x, T.x);
-            x2 = xsub(S.y, T.y);
-        } else {
-            x1 = xadd(xsub(S.x, T.x), z.x);
-            x2 = xadd(xsub(S.y, T.y), z.y);
-        }
-        const double r2 = xadd(xmul(x1, x1), xmul(x2, x2));
-        const double e2 = exp(-a.xi2 * r2);
-        const double pf = 2.0 * a.xi2;
-        const double fb = -4.0 * (1.0 + a.xi2 * r2) / r2 / r2;
         const double *Sc = a.coef + (int64_t)a.nc * s + a.doff;
         const double S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2];
-        const double T111 = x1 * x1 * x1 * fb + pf * 3.0 * x1;
-        const double T112 = x1 * x1 * x2 * fb + pf * x2;
-        const double T122 = x1 * x2 * x2 * fb + pf * x1;
-        const double T222 = x2 * x2 * x2 * fb + pf * 3.0 * x2;
-        d1 += e2 * (T111 * S11 + T112 * S1221 + T122 * S22);
-        d2 += e2 * (T112 * S11 + T122 * S1221 + T222 * S22);
+        const double r2d = fma(x1, x1, x2 * x2);
+        double xd = x, exd = ex, ird = ir2;
+        if (r2d != r2) {
+            xd = r2d * a.xi2;
+            exd = exp_neg(xd, tab);
+            ird = rcp_nr(r2d);
+        }
+        const double fb = -4.0 * (1.0 + xd) * ird * ird;
+        const double Q = fma(x1 * x1, S11, fma(x1 * x2, S1221, x2 * x2 * S22));
+        const double A1 = fma(x1, fma(3.0, S11, S22), x2 * S1221);
+        const double A2 = fma(x2, fma(3.0, S22, S11), x1 * S1221);
+        const double fq = fb * Q, pf = a.pf;
+        d1 = fma(exd, fma(fq, x1, pf * A1), d1);
+        d2 = fma(exd, fma(fq, x2, pf * A2), d2);
     }
 }
 
 template <bool SLP, bool DLP>
 __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
 {
-    __shared__ int2 q[kRealWarps][64];
-    __shared__ int nbb[kRealWarps][9];
-    __shared__ double2 nbz[kRealWarps][9];
+    __shared__ RealWarp warps[kRealWarps];
+    __shared__ double tab[64];
+    __shared__ double e1s[66];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
+    for (int i = threadIdx.x; i < 66; i += blockDim.x) e1s[i] = (&c_e1[0][0])[i];
+    __syncthreads();
+    RealWarp &W = warps[wid];
     const int64_t nw = (int64_t)gridDim.x * kRealWarps;
-    for (int64_t t = (int64_t)blockIdx.x * kRealWarps + wid; t < a.ntar; t += nw) {
-        const int tb = a.tbox[t];
-        const int bx = tb % a.nx, by = tb / a.nx;
-        if (lane < 9) {
-            const int ux = bx + c_nb_dx[lane], uy = by + c_nb_dy[lane];
-            const int wx = (ux + a.nx) % a.nx, wy = (uy + a.ny) % a.ny;
-            nbb[wid][lane] = wy * a.nx + wx;
-            nbz[wid][lane] = make_double2(xdiv(xmul(a.Lx, (double)(ux - wx)), (double)a.nx),
-                                          xdiv(xmul(a.Ly, (double)(uy - wy)), (double)a.ny));
+
+    int qn = 0, head = 0, nfl = 0, gseq = 0;   // queue count, ring head, in flight, targets started
+    long long enq = 0, proc = 0;
+    int tag = -1;                               // target sequence number of the lane's sums
+    double s1 = 0, s2 = 0, d1 = 0, d2 = 0;
+    unsigned long long ncand = 0, nslp = 0, ndlp = 0;
+
+    // Evaluate the first cnt queued pairs (lanes >= cnt idle), flushing lanes
+    // whose sums belong to another target first.
+    auto batch = [&](int cnt) {
+        const int2 e = lane < cnt ? W.q[lane] : make_int2(0, -1);
+        __syncwarp();
+        if (lane < qn - cnt) W.q[lane] = W.q[lane + cnt];
+        qn -= cnt;
+        proc += cnt;
+        // target sequence number of the entry: slot -> ring position -> sequence
+        int eseq = -1;
+        if (e.y >= 0) {
+            const int slot = e.y & 0xff;
+            eseq = gseq - nfl + ((slot - head + kRing) % kRing);
+        }
+        const bool fl = tag >= 0 && (lane >= cnt || tag != eseq);
+        if (__any_sync(~0u, fl)) {
+            seg_flush(W, lane, tag, fl ? s1 : 0.0, fl ? s2 : 0.0, fl ? d1 : 0.0, fl ? d2 : 0.0);
+            if (fl) {
+                s1 = s2 = d1 = d2 = 0.0;
+                tag = -1;
+            }
+        }
+        if (lane < cnt) {
+            real_pair<SLP, DLP>(a, W, e, tab, e1s, s1, s2, d1, d2);
+            tag = eseq;
+        }
+    };
+    // Retire finished targets in order (or all, after a full flush).
+    auto retire = [&](bool all) {
+        while (nfl > 0 && (all || proc >= W.tend[head] + 32)) {
+            if (lane == 0) {
+                const long long t = W.tidx[head];
+                if (SLP) a.u_slp[t] = make_double2(W.acc[head][0], W.acc[head][1]);
+                if (DLP) a.u_dlp[t] = make_double2(W.acc[head][2], W.acc[head][3]);
+            }
+            head = (head + 1) % kRing;
+            nfl--;
         }
         __syncwarp();
+    };
+    auto drain = [&]() {
+        batch(qn);
+        const int key = tag >= 0 ? tag : 0x7fffffff;
+        seg_flush(W, lane, key, s1, s2, d1, d2);
+        s1 = s2 = d1 = d2 = 0.0;
+        tag = -1;
+        retire(true);
+    };
+
+    for (int64_t t = (int64_t)blockIdx.x * kRealWarps + wid; t < a.ntar; t += nw) {
+        if (nfl == kRing) drain();
+        const int slot = (head + nfl) % kRing;
+        nfl++;
+        gseq++;
+        const int tb = a.tbox[t];
         const double2 T = a.tp[t];
-        double s1 = 0.0, s2 = 0.0, d1 = 0.0, d2 = 0.0;
-        int qn = 0;
-        for (int k = 0; k < 9; k++) {
-            const int sb = nbb[wid][k];
-            const int b0 = a.sstart[sb], b1 = a.sstart[sb + 1];
-            const double2 z = nbz[wid][k];
-            for (int base = b0; base < b1; base += 32) {
-                const int s = base + lane;
-                int fl = 0;
-                if (s < b1) {
+        const float2 Tf = a.tpf[t];
+        if (lane < 4) W.acc[slot][lane] = 0.0;
+        if (lane == 0) {
+            W.tpos[slot] = T;
+            W.tbox[slot] = tb;
+            W.tidx[slot] = t;
+        }
+        // neighbour boxes: first source, counts -> list prefix, image shift
+        int cntk = 0;
+        if (lane < 9) {
+            const int ux = tb % a.nx + c_nb_dx[lane], uy = tb / a.nx + c_nb_dy[lane];
+            const int wx = (ux + a.nx) % a.nx, wy = (uy + a.ny) % a.ny;
+            const int sb = wy * a.nx + wx;
+            const int b0 = a.sstart[sb];
+            cntk = a.sstart[sb + 1] - b0;
+            W.nbs[lane] = b0;
+            const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+            const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+            W.nbz[lane] = make_double2(zx, zy);
+            W.nbzf[lane] = make_float2((float)zx, (float)zy);
+        }
+        int incl = cntk;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const int v = __shfl_up_sync(~0u, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane < 9) W.nbp[lane + 1] = incl;
+        if (lane == 0) W.nbp[0] = 0;
+        __syncwarp();
+        const int total = W.nbp[9];
+        ncand += (unsigned)total;
+        for (int v0 = 0; v0 < total; v0 += 32) {
+            const int v = v0 + lane;
+            int fl = 0, s = 0, k = 0;
+            if (v < total) {
+                while (v >= W.nbp[k + 1]) k++;
+                s = W.nbs[k] + (v - W.nbp[k]);
+                if (k == 0) {
                     const double2 S = a.sp[s];
-                    if (k == 0) {
-                        const double dx = xsub(T.x, S.x), dy = xsub(T.y, S.y);
-                        const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
-                        if (r2 == 0.0) {
-                            // SLP self term (mex_stokes_slp_real.cpp:161-163); DLP skips r2 == 0.
-                            if (SLP) {
-                                const double *f = a.coef + (int64_t)a.nc * s;
-                                s1 += a.self_c * f[0];
-                                s2 += a.self_c * f[1];
-                            }
-                        } else {
-                            fl = 3;
+                    const double dx = xsub(T.x, S.x), dy = xsub(T.y, S.y);
+                    if (xadd(xmul(dx, dx), xmul(dy, dy)) == 0.0) {
+                        // SLP self term (mex_stokes_slp_real.cpp:161-163); DLP skips r2 == 0.
+                        if (SLP) {
+                            const double *f = a.coef + (int64_t)a.nc * s;
+                            atomicAdd(&W.acc[slot][0], a.self_c * f[0]);
+                            atomicAdd(&W.acc[slot][1], a.self_c * f[1]);
                         }
                     } else {
+                        fl = 3;
+                    }
+                } else {
+                    const float2 Sf = a.spf[s];
+                    const float2 zf = W.nbzf[k];
+                    const float dxf = Sf.x - (Tf.x - zf.x), dyf = Sf.y - (Tf.y - zf.y);
+                    const float r2f = dxf * dxf + dyf * dyf;
+                    // |r2f - r2| bound for both offset forms (3 roundings per
+                    // coordinate, then squaring and summing), doubled.
+                    const float ex = 0x1p-22f * (fabsf(Sf.x) + fabsf(Tf.x) + fabsf(zf.x));
+                    const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
+                    const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
+                                               ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
+                    if (r2f + band < a.cut2f) {
+                        fl = 3;
+                    } else if (!(r2f - band >= a.cut2f)) {
+                        // near the cutoff (or non-finite): the reference's exact tests
+                        const double2 S = a.sp[s];
+                        const double2 z = W.nbz[k];
                         if (SLP) {
                             const double dx = xsub(S.x, xsub(T.x, z.x));
                             const double dy = xsub(S.y, xsub(T.y, z.y));
@@ -242,42 +535,27 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                         }
                     }
                 }
-                const unsigned m = __ballot_sync(~0u, fl != 0);
-                if (fl) q[wid][qn + __popc(m & ((1u << lane) - 1u))] = make_int2(s, (k << 2) | fl);
-                qn += __popc(m);
-                __syncwarp();
-                if (qn >= 32) {
-                    const int2 e = q[wid][lane];
-                    __syncwarp();
-                    if (lane < qn - 32) q[wid][lane] = q[wid][lane + 32];
-                    qn -= 32;
-                    const int kk = e.y >> 2;
-                    real_pair<SLP, DLP>(a, e.x, kk, e.y & 3, T, nbz[wid][kk], s1, s2, d1, d2);
-                    __syncwarp();
-                }
             }
+            if (!SLP) fl &= 2;
+            if (!DLP) fl &= 1;
+            const unsigned m = __ballot_sync(~0u, fl != 0);
+            nslp += __popc(__ballot_sync(~0u, (fl & 1) != 0));
+            ndlp += __popc(__ballot_sync(~0u, (fl & 2) != 0));
+            if (fl) W.q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(s, slot | (k << 8) | (fl << 12));
+            qn += __popc(m);
+            enq += __popc(m);
+            __syncwarp();
+            if (qn >= 32) batch(32);
         }
-        if (lane < qn) {
-            const int2 e = q[wid][lane];
-            const int kk = e.y >> 2;
-            real_pair<SLP, DLP>(a, e.x, kk, e.y & 3, T, nbz[wid][kk], s1, s2, d1, d2);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            if (SLP) {
-                s1 += __shfl_xor_sync(~0u, s1, o);
-                s2 += __shfl_xor_sync(~0u, s2, o);
-            }
-            if (DLP) {
-                d1 += __shfl_xor_sync(~0u, d1, o);
-                d2 += __shfl_xor_sync(~0u, d2, o);
-            }
-        }
-        if (lane == 0) {
-            if (SLP) a.u_slp[t] = make_double2(s1, s2);
-            if (DLP) a.u_dlp[t] = make_double2(d1, d2);
-        }
+        if (lane == 0) W.tend[slot] = enq;
         __syncwarp();
+        retire(false);
+    }
+    drain();
+    if (a.counters && lane == 0) {
+        atomicAdd(a.counters, ncand);
+        if (SLP) atomicAdd(a.counters + 1, nslp);
+        if (DLP) atomicAdd(a.counters + 2, ndlp);
     }
 }
 
@@ -708,7 +986,8 @@ static int sm_count()
 }
 
 cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *sorted_box,
-                       double2 *sorted_pos, cudaStream_t st, int64_t &launches)
+                       double2 *sorted_pos, float2 *sorted_pos_f, cudaStream_t st,
+                       int64_t &launches)
 {
     cudaError_t e = cudaMemsetAsync(a.count, 0, sizeof(int) * (size_t)nbox, st);
     if (e != cudaSuccess) return e;
@@ -720,7 +999,8 @@ cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *s
     launches++;
     if (a.n > 0) {
         k_bin_place<<<grid_for(a.n, 256), 256, 0, st>>>(a.n, a.box, a.rank, start, perm,
-                                                         sorted_box, a.p, sorted_pos);
+                                                         sorted_box, a.p, sorted_pos,
+                                                         sorted_pos_f);
         launches++;
     }
     return cudaGetLastError();

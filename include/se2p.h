@@ -67,6 +67,24 @@ int64_t se2p_plan_workspace_bytes(se2p_plan plan);
 int64_t se2p_plan_kernel_launches(se2p_plan plan);
 const char *se2p_version(void);
 
+/* ---- stage timing ------------------------------------------------------------
+ * Replaces the drivers' `verbose` tic/toc prints (StokesSLP_ewald_2p.m:106-131):
+ * with timing on, every stage of every call (h2d, wrap, sort, coef, real,
+ * spread, fft_fwd, filter, fft_inv, gather, zero_mode, assemble, d2h) is
+ * bracketed by CUDA events on the plan's stream.  se2p_plan_stage_times
+ * waits for the pending events and returns, per stage, the accumulated
+ * milliseconds and call counts (arrays of se2p_num_stages() entries). */
+int se2p_plan_enable_timing(se2p_plan plan, int on);
+int se2p_num_stages(void);
+const char *se2p_stage_name(int stage);
+int se2p_plan_stage_times(se2p_plan plan, double *ms, int64_t *calls, int reset);
+
+/* Real-space work counters: with counting on, the real-space kernel adds up
+ * per call the candidate sources it examined and the SLP and DLP pairs it
+ * accepted.  Sets counting on/off and returns the totals so far in
+ * counts[3] = {candidates, slp_pairs, dlp_pairs} (optionally resetting them). */
+int se2p_plan_count_pairs(se2p_plan plan, int on, int64_t *counts, int reset);
+
 /* ---- MEX gateways ----------------------------------------------------------
  * Replaces mex_stokes_slp_real(psrc, ptar, f, xi, nside_x, nside_y, Lx, Ly)
  * (PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_real.cpp:58-83). */
