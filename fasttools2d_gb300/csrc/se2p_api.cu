@@ -58,6 +58,8 @@ struct se2p_plan_st {
     int device = 0;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;     // real space runs here, concurrently with k space
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::string err;
     int64_t launches = 0;
     DevBuf buf[S_COUNT_SLOTS];
@@ -106,21 +108,23 @@ int fail(se2p_plan pl, int code, const char *fmt, ...)
 struct StageTimer {
     se2p_plan pl;
     int stage;
+    cudaStream_t st;
     cudaEvent_t a = nullptr, b = nullptr;
-    StageTimer(se2p_plan p, int st) : pl(p), stage(st)
+    StageTimer(se2p_plan p, int stg, cudaStream_t s = nullptr) : pl(p), stage(stg)
     {
+        st = s ? s : pl->stream;
         if (!pl->timing) return;
         if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
             cudaGetLastError();
             a = b = nullptr;
             return;
         }
-        cudaEventRecord(a, pl->stream);
+        cudaEventRecord(a, st);
     }
     ~StageTimer()
     {
         if (!a) return;
-        cudaEventRecord(b, pl->stream);
+        cudaEventRecord(b, st);
         pl->pending[stage].emplace_back(a, b);
     }
 };
@@ -146,6 +150,7 @@ int ensure(se2p_plan pl, int slot, size_t bytes, void **out)
     if (b.bytes < bytes) {
         if (b.p) {
             CK(cudaStreamSynchronize(pl->stream));
+            if (pl->side) CK(cudaStreamSynchronize(pl->side));
             CK(cudaFree(b.p));
             b.p = nullptr;
             b.bytes = 0;
@@ -436,6 +441,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ra.xi2 = J.xi * J.xi;
         ra.cut2 = J.Lx * J.Ly / nx / ny;                 // mex_stokes_slp_real.cpp:127
         ra.cut2f = (float)ra.cut2;
+        ra.xi2f = (float)(J.xi * J.xi);
         ra.inv_xi2 = 1.0 / (J.xi * J.xi);
         ra.pf = 2.0 * J.xi * J.xi;
         // (len*(per_source - t))/nside with per_source - t = -+nside
@@ -456,8 +462,17 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             }
             ra.counters = static_cast<unsigned long long *>(pl->buf[S_COUNTERS].p);
         }
-        StageTimer tm(pl, T_REAL);
-        CK(launch_real(ra, J.slp, J.dlp, st, pl->launches));
+        // Real space on the side stream, overlapping the k-space chain.
+        cudaStream_t rs = J.kspace ? pl->side : st;
+        if (J.kspace) {
+            CK(cudaEventRecord(pl->fork, st));
+            CK(cudaStreamWaitEvent(rs, pl->fork, 0));
+        }
+        {
+            StageTimer tm(pl, T_REAL, rs);
+            CK(launch_real(ra, J.slp, J.dlp, rs, pl->launches));
+        }
+        if (J.kspace) CK(cudaEventRecord(pl->join, rs));
     }
 
     if (J.kspace) {
@@ -559,6 +574,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         CK(launch_zero_mode(ns, ps, fd, nr, 1.0 / (J.Lx * J.Ly), part, zm, st, pl->launches));
     }
 
+    if (J.real && J.kspace) CK(cudaStreamWaitEvent(st, pl->join, 0));
     StageTimer *t_asm = new StageTimer(pl, T_ASSEMBLE);
     const double2 *uk_slp = (J.kspace && J.slp) ? uk : nullptr;
     const double2 *uk_dlp = (J.kspace && J.dlp) ? uk + (J.slp ? nt : 0) : nullptr;
@@ -610,6 +626,13 @@ int se2p_plan_create(se2p_plan *plan, int device)
         return SE2P_ERR_CUDA;
     }
     pl->stream = pl->own;
+    if (cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        se2p_plan_destroy(pl);
+        return SE2P_ERR_CUDA;
+    }
     *plan = pl;
     return SE2P_OK;
 }
@@ -627,6 +650,12 @@ int se2p_plan_destroy(se2p_plan pl)
     for (auto &kv : pl->ffts) cufftDestroy(kv.second);
     for (auto &b : pl->buf)
         if (b.p) cudaFree(b.p);
+    if (pl->side) {
+        cudaStreamSynchronize(pl->side);
+        cudaStreamDestroy(pl->side);
+    }
+    if (pl->fork) cudaEventDestroy(pl->fork);
+    if (pl->join) cudaEventDestroy(pl->join);
     if (pl->own) cudaStreamDestroy(pl->own);
     delete pl;
     return SE2P_OK;

@@ -142,7 +142,7 @@ struct RealArgs {
     double Lx, Ly, xi, xi2, cut2, self_c;
     double inv_xi2, pf;   // 1/xi^2, 2 xi^2
     double zxm, zxp, zym, zyp;   // image shifts (L*(-+nside))/nside of the wrapped neighbours
-    float cut2f;
+    float cut2f, xi2f;
     double2 *u_slp;       // raw sums per sorted target (no 1/(4 pi))
     double2 *u_dlp;
     unsigned long long *counters;   // [candidates, SLP pairs, DLP pairs] (may be NULL)

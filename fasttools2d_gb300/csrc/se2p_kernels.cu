@@ -284,19 +284,20 @@ __device__ __forceinline__ double rcp_nr(double a)
 }
 
 struct RealWarp {
-    int2 q[64];                 // (sorted source, slot | k << 8 | flags << 12)
+    int2 q[2][64];              // pair FIFOs: [0] main, [1] near field (x <= 1)
+                                // entry = (sorted source, slot | k << 8 | flags << 12)
     double acc[kRing][4];       // per-target sums: SLP u1, u2, DLP u1, u2
     double2 tpos[kRing];
     int tbox[kRing];
     long long tidx[kRing];
-    long long tend[kRing];      // queue position after the target's last pair
+    long long tend[2][kRing];   // FIFO position after the target's last pair
     int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
     double2 nbz[9];
     float2 nbzf[9];
 };
 
 // Segmented warp reduction of (v0..v3) by nondecreasing key; the last lane
-// of each segment with key >= 0 adds its sum into the ring slot key % kRing.
+// of each segment with a real key adds its sum into ring slot key % kRing.
 __device__ __forceinline__ void seg_flush(RealWarp &W, int lane, int key, double v0, double v1,
                                           double v2, double v3)
 {
@@ -380,6 +381,14 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
     }
 }
 
+// Lane-side state of one pair FIFO.
+struct PairQueue {
+    int qn;               // entries queued (warp-uniform)
+    long long enq, proc;  // entries enqueued / processed so far (warp-uniform)
+    int tag;              // sequence number of the target this lane's sums belong to
+    double s1, s2, d1, d2;
+};
+
 template <bool SLP, bool DLP>
 __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
 {
@@ -393,42 +402,44 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
     RealWarp &W = warps[wid];
     const int64_t nw = (int64_t)gridDim.x * kRealWarps;
 
-    int qn = 0, head = 0, nfl = 0, gseq = 0;   // queue count, ring head, in flight, targets started
-    long long enq = 0, proc = 0;
-    int tag = -1;                               // target sequence number of the lane's sums
-    double s1 = 0, s2 = 0, d1 = 0, d2 = 0;
+    int head = 0, nfl = 0, gseq = 0;   // ring head slot, targets in flight, targets started
+    PairQueue Q[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        Q[j].qn = 0; Q[j].enq = 0; Q[j].proc = 0; Q[j].tag = -1;
+        Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
+    }
     unsigned long long ncand = 0, nslp = 0, ndlp = 0;
 
-    // Evaluate the first cnt queued pairs (lanes >= cnt idle), flushing lanes
-    // whose sums belong to another target first.
-    auto batch = [&](int cnt) {
-        const int2 e = lane < cnt ? W.q[lane] : make_int2(0, -1);
+    // Evaluate the first cnt pairs of FIFO j (lanes >= cnt idle); lanes whose
+    // sums belong to another target flush first.
+    auto batch = [&](int j, int cnt) {
+        PairQueue &P = Q[j];
+        const int2 e = lane < cnt ? W.q[j][lane] : make_int2(0, -1);
         __syncwarp();
-        if (lane < qn - cnt) W.q[lane] = W.q[lane + cnt];
-        qn -= cnt;
-        proc += cnt;
-        // target sequence number of the entry: slot -> ring position -> sequence
+        if (lane < P.qn - cnt) W.q[j][lane] = W.q[j][lane + cnt];
+        P.qn -= cnt;
+        P.proc += cnt;
         int eseq = -1;
-        if (e.y >= 0) {
-            const int slot = e.y & 0xff;
-            eseq = gseq - nfl + ((slot - head + kRing) % kRing);
-        }
-        const bool fl = tag >= 0 && (lane >= cnt || tag != eseq);
+        if (e.y >= 0) eseq = gseq - nfl + (((e.y & 0xff) - head + kRing) % kRing);
+        const bool fl = P.tag >= 0 && (lane >= cnt || P.tag != eseq);
         if (__any_sync(~0u, fl)) {
-            seg_flush(W, lane, tag, fl ? s1 : 0.0, fl ? s2 : 0.0, fl ? d1 : 0.0, fl ? d2 : 0.0);
+            seg_flush(W, lane, P.tag, fl ? P.s1 : 0.0, fl ? P.s2 : 0.0, fl ? P.d1 : 0.0,
+                      fl ? P.d2 : 0.0);
             if (fl) {
-                s1 = s2 = d1 = d2 = 0.0;
-                tag = -1;
+                P.s1 = P.s2 = P.d1 = P.d2 = 0.0;
+                P.tag = -1;
             }
         }
         if (lane < cnt) {
-            real_pair<SLP, DLP>(a, W, e, tab, e1s, s1, s2, d1, d2);
-            tag = eseq;
+            real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
+            P.tag = eseq;
         }
     };
-    // Retire finished targets in order (or all, after a full flush).
+    // Retire finished targets in order (all of them after a full flush).
     auto retire = [&](bool all) {
-        while (nfl > 0 && (all || proc >= W.tend[head] + 32)) {
+        while (nfl > 0 && (all || (Q[0].proc >= W.tend[0][head] + 32 &&
+                                   Q[1].proc >= W.tend[1][head] + 32))) {
             if (lane == 0) {
                 const long long t = W.tidx[head];
                 if (SLP) a.u_slp[t] = make_double2(W.acc[head][0], W.acc[head][1]);
@@ -440,11 +451,14 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         __syncwarp();
     };
     auto drain = [&]() {
-        batch(qn);
-        const int key = tag >= 0 ? tag : 0x7fffffff;
-        seg_flush(W, lane, key, s1, s2, d1, d2);
-        s1 = s2 = d1 = d2 = 0.0;
-        tag = -1;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            batch(j, Q[j].qn);
+            const int key = Q[j].tag >= 0 ? Q[j].tag : 0x7fffffff;
+            seg_flush(W, lane, key, Q[j].s1, Q[j].s2, Q[j].d1, Q[j].d2);
+            Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
+            Q[j].tag = -1;
+        }
         retire(true);
     };
 
@@ -490,13 +504,15 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         for (int v0 = 0; v0 < total; v0 += 32) {
             const int v = v0 + lane;
             int fl = 0, s = 0, k = 0;
+            bool nearp = false;
             if (v < total) {
                 while (v >= W.nbp[k + 1]) k++;
                 s = W.nbs[k] + (v - W.nbp[k]);
                 if (k == 0) {
                     const double2 S = a.sp[s];
                     const double dx = xsub(T.x, S.x), dy = xsub(T.y, S.y);
-                    if (xadd(xmul(dx, dx), xmul(dy, dy)) == 0.0) {
+                    const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
+                    if (r2 == 0.0) {
                         // SLP self term (mex_stokes_slp_real.cpp:161-163); DLP skips r2 == 0.
                         if (SLP) {
                             const double *f = a.coef + (int64_t)a.nc * s;
@@ -505,6 +521,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                         }
                     } else {
                         fl = 3;
+                        nearp = (float)r2 * a.xi2f <= 1.0f;
                     }
                 } else {
                     const float2 Sf = a.spf[s];
@@ -517,6 +534,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                     const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
                     const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
                                                ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
+                    nearp = r2f * a.xi2f <= 1.0f;
                     if (r2f + band < a.cut2f) {
                         fl = 3;
                     } else if (!(r2f - band >= a.cut2f)) {
@@ -538,16 +556,25 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
             }
             if (!SLP) fl &= 2;
             if (!DLP) fl &= 1;
-            const unsigned m = __ballot_sync(~0u, fl != 0);
             nslp += __popc(__ballot_sync(~0u, (fl & 1) != 0));
             ndlp += __popc(__ballot_sync(~0u, (fl & 2) != 0));
-            if (fl) W.q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(s, slot | (k << 8) | (fl << 12));
-            qn += __popc(m);
-            enq += __popc(m);
+            const int2 ent = make_int2(s, slot | (k << 8) | (fl << 12));
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const bool mine = fl != 0 && nearp == (j == 1);
+                const unsigned m = __ballot_sync(~0u, mine);
+                if (mine) W.q[j][Q[j].qn + __popc(m & ((1u << lane) - 1u))] = ent;
+                Q[j].qn += __popc(m);
+                Q[j].enq += __popc(m);
+            }
             __syncwarp();
-            if (qn >= 32) batch(32);
+            if (Q[0].qn >= 32) batch(0, 32);
+            if (Q[1].qn >= 32) batch(1, 32);
         }
-        if (lane == 0) W.tend[slot] = enq;
+        if (lane == 0) {
+            W.tend[0][slot] = Q[0].enq;
+            W.tend[1][slot] = Q[1].enq;
+        }
         __syncwarp();
         retire(false);
     }
