@@ -14,6 +14,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libse2p.so")
 
 SE2P_OK, SE2P_ERR_ARG, SE2P_ERR_CUDA, SE2P_ERR_CUFFT, SE2P_ERR_ALLOC, SE2P_ERR_UNSUPPORTED = range(6)
+NOALLOC_SCRATCH_BYTES = 32 << 20   # SE2P_NOALLOC_SCRATCH_BYTES
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_CUFFT", 4: "ERR_ALLOC",
                 5: "ERR_UNSUPPORTED"}
 
@@ -24,7 +25,7 @@ EXPORTS = (
     "se2p_slp_real", "se2p_slp_kspace", "se2p_dlp_real", "se2p_dlp_kspace",
     "se2p_slp_ewald", "se2p_dlp_ewald", "se2p_stokes_ewald",
     "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
-    "se2p_plan_count_pairs",
+    "se2p_plan_count_pairs", "se2p_slp_real_noalloc",
 )
 
 
@@ -79,6 +80,7 @@ def load(path: str = LIB_PATH):
         L.se2p_plan_stage_times.argtypes = [P, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_int64), i32]
         L.se2p_plan_count_pairs.argtypes = [P, i32, ctypes.POINTER(ctypes.c_int64), i32]
+        L.se2p_slp_real_noalloc.argtypes = [_dp, i64, _dp, i64, _dp, d, i32, i32, d, d, _dp, P]
         PP = ctypes.POINTER(Params)
         L.se2p_slp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp]
         L.se2p_dlp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp]

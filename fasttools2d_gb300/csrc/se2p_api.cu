@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -871,3 +872,143 @@ int se2p_stokes_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, 
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free SLP real space (se2p_slp_real_noalloc)
+//
+// For callers that cannot call cudaMalloc (MATLAB MEX code whose GPU memory
+// belongs to gpuArray's allocator; solver loops that must not allocate).  The
+// working arrays of one call are carved from this fixed device array, which
+// each GPU that loads the library keeps until exit.  In host code the name
+// g_noalloc_scratch is only a host-side stand-in: its device address comes
+// from cudaGetSymbolAddress, once per device, with that device current.
+// ============================================================================
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SE2P_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256] = {nullptr};
+
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Bytes of scratch one call needs (the carve order of se2p_slp_real_noalloc).
+size_t noalloc_bytes(int64_t ns, int64_t nt, int64_t nbox)
+{
+    const size_t s = (size_t)(ns > 0 ? ns : 1), t = (size_t)nt, b = (size_t)nbox;
+    return round256(4 * s) * 3 + round256(4 * t) * 4 + round256(4 * b) + 2 * round256(4 * (b + 1)) +
+           round256(16 * s) + round256(16 * t) + round256(8 * s) + round256(8 * t) +
+           round256(16 * s) + round256(16 * t);
+}
+
+bool on_device(const void *p, int dev)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) &&
+           at.device == dev && (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+}  // namespace
+
+extern "C" int se2p_slp_real_noalloc(const double *psrc, int64_t ns, const double *ptar,
+                                     int64_t nt, const double *f, double xi, int nside_x,
+                                     int nside_y, double Lx, double Ly, double *u,
+                                     void *cuda_stream)
+{
+    if (ns < 0 || nt < 0 || nside_x < 1 || nside_y < 1) return SE2P_ERR_ARG;
+    if (!(std::isfinite(xi) && xi > 0 && std::isfinite(Lx) && Lx > 0 && std::isfinite(Ly) && Ly > 0))
+        return SE2P_ERR_ARG;
+    if (nt == 0) return SE2P_OK;
+    const int64_t nbox = (int64_t)nside_x * nside_y;
+    if (ns > 0x7fffffff || nt > 0x7fffffff || nbox > (1 << 26) ||
+        noalloc_bytes(ns, nt, nbox) > SE2P_NOALLOC_SCRATCH_BYTES)
+        return SE2P_ERR_UNSUPPORTED;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        cudaGetLastError();
+        return SE2P_ERR_CUDA;
+    }
+    if (!ptar || !u || !on_device(ptar, dev) || !on_device(u, dev)) return SE2P_ERR_ARG;
+    if (ns > 0 && (!psrc || !f || !on_device(psrc, dev) || !on_device(f, dev))) return SE2P_ERR_ARG;
+
+    unsigned char *base;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return SE2P_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = p;
+        }
+        base = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+    }
+    const size_t s1 = (size_t)(ns > 0 ? ns : 1), t1 = (size_t)nt;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        void *p = base + off;
+        off += round256(bytes);
+        return p;
+    };
+    int *sbox = (int *)carve(4 * s1), *srank = (int *)carve(4 * s1), *sperm = (int *)carve(4 * s1);
+    int *tbox = (int *)carve(4 * t1), *trank = (int *)carve(4 * t1), *tperm = (int *)carve(4 * t1);
+    int *tboxs = (int *)carve(4 * t1);
+    int *count = (int *)carve(4 * (size_t)nbox);
+    int *sstart = (int *)carve(4 * ((size_t)nbox + 1)), *tstart = (int *)carve(4 * ((size_t)nbox + 1));
+    double2 *sp = (double2 *)carve(16 * s1), *tp = (double2 *)carve(16 * t1);
+    float2 *spf = (float2 *)carve(8 * s1), *tpf = (float2 *)carve(8 * t1);
+    double *coef = (double *)carve(16 * s1);
+    double2 *ur = (double2 *)carve(16 * t1);
+
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    int64_t launches = 0;
+    const double2 *ps = reinterpret_cast<const double2 *>(psrc);
+    const double2 *pt = reinterpret_cast<const double2 *>(ptar);
+    BinArgs bs{ps, ns, Lx, Ly, nside_x, nside_y, sbox, srank, count};
+    if (launch_bin(bs, sstart, (int)nbox, sperm, nullptr, sp, spf, st, launches) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+    BinArgs bt{pt, nt, Lx, Ly, nside_x, nside_y, tbox, trank, count};
+    if (launch_bin(bt, tstart, (int)nbox, tperm, tboxs, tp, tpf, st, launches) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+    if (launch_src_coef(ns, sperm, reinterpret_cast<const double2 *>(f), nullptr, nullptr, coef,
+                        2, st, launches) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+    RealArgs ra;
+    ra.sp = sp;
+    ra.spf = spf;
+    ra.tpf = tpf;
+    ra.coef = coef;
+    ra.nc = 2;
+    ra.doff = 0;
+    ra.sstart = sstart;
+    ra.tp = tp;
+    ra.tbox = tboxs;
+    ra.ntar = nt;
+    ra.nx = nside_x;
+    ra.ny = nside_y;
+    ra.Lx = Lx;
+    ra.Ly = Ly;
+    ra.xi = xi;
+    ra.xi2 = xi * xi;
+    ra.cut2 = Lx * Ly / nside_x / nside_y;                 // mex_stokes_slp_real.cpp:127
+    ra.cut2f = (float)ra.cut2;
+    ra.xi2f = (float)(xi * xi);
+    ra.inv_xi2 = 1.0 / (xi * xi);
+    ra.pf = 2.0 * xi * xi;
+    ra.zxm = (Lx * (double)(-nside_x)) / nside_x;
+    ra.zxp = (Lx * (double)nside_x) / nside_x;
+    ra.zym = (Ly * (double)(-nside_y)) / nside_y;
+    ra.zyp = (Ly * (double)nside_y) / nside_y;
+    ra.self_c = -1.288607832450766155 - std::log(xi);   // mex_stokes_slp_real.cpp:124
+    ra.u_slp = ur;
+    ra.u_dlp = nullptr;
+    ra.counters = nullptr;
+    if (launch_real(ra, true, false, st, launches) != cudaSuccess) return SE2P_ERR_CUDA;
+    if (launch_assemble(nt, 0, tperm, ur, nullptr, nullptr, reinterpret_cast<double2 *>(u), nullptr,
+                        nullptr, st, launches) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+    return SE2P_OK;
+}

@@ -134,6 +134,33 @@ int se2p_stokes_ewald(se2p_plan plan, const se2p_params *prm, const double *psrc
                       int64_t nsrc, const double *ptar, int64_t ntar, const double *f_slp,
                       const double *f_dlp, const double *n, double *u_slp, double *u_dlp);
 
+/* ---- allocation-free SLP real space ------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a MEX function running inside MATLAB, where gpuArray's caching
+ * allocator owns the GPU's memory, or a solver's time-step loop that must not
+ * stall or fail on cudaMalloc.  Computes exactly what se2p_slp_real computes,
+ * but all working arrays live in one fixed file-scope device array of
+ * SE2P_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU which loads this library
+ * holds until the process exits; nothing is allocated or freed per call.
+ *
+ *  - psrc, ptar, f and u must be device memory of the current device,
+ *    16-byte aligned; the work is queued on `cuda_stream` (NULL = legacy
+ *    default stream) and the call returns without synchronising.
+ *  - Size limit: 256-byte-rounded arrays totalling about
+ *    52*nsrc + 56*ntar + 12*nside_x*nside_y bytes must fit in 32 MiB
+ *    (e.g. 290,000 sources plus 290,000 targets with nside 178); larger
+ *    calls return SE2P_ERR_UNSUPPORTED before touching the GPU.
+ *  - The first call on each device resolves the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - Every call reuses the same array, which keeps the previous call's
+ *    contents (the per-box counters are cleared on each call); calls whose
+ *    GPU work overlaps, on any stream or thread, race on it. */
+#define SE2P_NOALLOC_SCRATCH_BYTES (32u << 20)
+int se2p_slp_real_noalloc(const double *psrc, int64_t nsrc, const double *ptar, int64_t ntar,
+                          const double *f, double xi, int nside_x, int nside_y, double Lx,
+                          double Ly, double *u, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
