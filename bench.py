@@ -242,6 +242,49 @@ def fp64_peak_tflops(torch, dev):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
+# Config 4: the mixed-precision workload (same points), tolerance 1e-6.
+XI4, RC4, M4, P4 = 860.0, 0.0042, 2048, 12
+
+
+def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
+    """FP32-grid vs FP64 on config 4: evals/s of each, speed-up, and the
+    FP32-grid error against the FP64 result per potential (max, RMS)."""
+    import torch
+    import fasttools2d_gb300 as ft
+    nside = int(math.floor(L / RC4))
+    prm4 = ft.EwaldParams.derived(XI4, nside, nside, M4, M4, P4, L, L).as_c()
+    L_ = plan.lib
+    out = {}
+    res = {}
+    for prec in ("fp64", "fp32_grid"):
+        plan.set_precision(prec)
+        u = [torch.empty_like(u_dev[0]), torch.empty_like(u_dev[1])]
+
+        def step():
+            plan.check(L_.se2p_stokes_ewald(plan.handle, ctypes.byref(prm4), tens[0].data_ptr(), N,
+                                            tens[1].data_ptr(), N, tens[2].data_ptr(),
+                                            tens[3].data_ptr(), tens[4].data_ptr(),
+                                            u[0].data_ptr(), u[1].data_ptr()))
+        for _ in range(3):
+            step()
+        ms = timed(step, steps) / steps
+        res[prec] = [x.double().cpu().numpy() for x in u]
+        out[prec] = {"evals_per_s": 1e3 / ms, "ms_per_step": ms}
+    plan.set_precision("fp64")
+    err = {}
+    for i, name in enumerate(("slp", "dlp")):
+        a, b = res["fp32_grid"][i], res["fp64"][i]
+        err[name] = {"max_rel": float(np.abs(a - b).max() / np.abs(b).max()),
+                     "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))}
+    return {"workload": f"config 4: same points, xi={XI4}, rc={RC4} (nside={nside}), M={M4}, "
+                        f"P={P4}, tol 1e-6",
+            "value": out["fp32_grid"]["evals_per_s"], "unit": UNIT,
+            "ms_per_step": out["fp32_grid"]["ms_per_step"],
+            "fp64_same_workload": out["fp64"],
+            "speedup_vs_fp64_same_workload": out["fp32_grid"]["evals_per_s"] / out["fp64"]["evals_per_s"],
+            "error_vs_fp64": err}
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -339,12 +382,28 @@ def gpu_arm(args, rank, world, local_rank):
            "h2d_bytes_per_step": 5 * N * 16, "d2h_bytes_per_step": 2 * N * 16,
            "ms_per_step": e2e_ms / args.steps}
 
+    # ---- per-kernel times without overlap (for the roofline) -------------
+    # Real space normally runs concurrently with the k-space chain; for the
+    # per-kernel roofline the stages are timed once more, in order.
+    plan.set_overlap(False)
+    plan.enable_timing(True)
+    plan.stage_times(reset=True)
+    for _ in range(2):
+        step_device()
+    torch.cuda.synchronize(dev)
+    stages = plan.stage_times(reset=True)
+    plan.enable_timing(False)
+    plan.set_overlap(True)
+
+    # ---- FP32-grid form (config 4) next to the FP64 form on the same workload
+    mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev)
+
     # ---- roofline of the dominant kernel ---------------------------------
     kstages = {k: v for k, v in stages.items() if k not in ("h2d", "d2h") and v[1] > 0}
     top = max(kstages, key=lambda k: kstages[k][0])
     top_ms = kstages[top][0] / kstages[top][1]
     peak = fp64_peak_tflops(torch, dev)
-    pairs_per_launch = (counts[1] + counts[2]) / max(1, kstages.get("real", (0, 1))[1])
+    pairs_per_launch = (counts[1] + counts[2]) / args.steps     # counted in the timed region
     real_ms = kstages["real"][0] / kstages["real"][1] if "real" in kstages else float("nan")
     real_flops = pairs_per_launch * REAL_FP64_FLOP_PER_PAIR
     roof = {"kernel": "k_real (fused SLP+DLP real-space pair sum)", "bound": "fp64",
@@ -354,7 +413,7 @@ def gpu_arm(args, rank, world, local_rank):
             "traffic": REAL_DRAM_BYTES, "traffic_unit": "bytes/launch (ncu)",
             "ms_per_launch": real_ms,
             "accepted_pairs_per_launch": pairs_per_launch,
-            "candidates_per_launch": counts[0] / max(1, kstages.get("real", (0, 1))[1]),
+            "candidates_per_launch": counts[0] / args.steps,
             "pairs_per_s": pairs_per_launch / (real_ms * 1e-3),
             "flop_per_pair": REAL_FP64_FLOP_PER_PAIR, "top_stage": top,
             "top_stage_ms": top_ms}
@@ -367,7 +426,7 @@ def gpu_arm(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config(N, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
         "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
-        "clocks": clk.summary(),
+        "clocks": clk.summary(), "fp32_grid": mixed,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N)

@@ -25,8 +25,10 @@ EXPORTS = (
     "se2p_slp_real", "se2p_slp_kspace", "se2p_dlp_real", "se2p_dlp_kspace",
     "se2p_slp_ewald", "se2p_dlp_ewald", "se2p_stokes_ewald",
     "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
-    "se2p_plan_count_pairs", "se2p_slp_real_noalloc",
+    "se2p_plan_count_pairs", "se2p_slp_real_noalloc", "se2p_plan_set_precision",
+    "se2p_plan_set_overlap",
 )
+PRECISION_FP64, PRECISION_FP32_GRID = 0, 1
 
 
 class Se2pError(RuntimeError):
@@ -80,6 +82,8 @@ def load(path: str = LIB_PATH):
         L.se2p_plan_stage_times.argtypes = [P, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_int64), i32]
         L.se2p_plan_count_pairs.argtypes = [P, i32, ctypes.POINTER(ctypes.c_int64), i32]
+        L.se2p_plan_set_precision.argtypes = [P, i32]
+        L.se2p_plan_set_overlap.argtypes = [P, i32]
         L.se2p_slp_real_noalloc.argtypes = [_dp, i64, _dp, i64, _dp, d, i32, i32, d, d, _dp, P]
         PP = ctypes.POINTER(Params)
         L.se2p_slp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp]
@@ -117,6 +121,15 @@ class Plan:
     @property
     def kernel_launches(self) -> int:
         return self.lib.se2p_plan_kernel_launches(self.handle)
+
+    def set_precision(self, precision):
+        """'fp64' (default) or 'fp32_grid' (mixed precision, tolerances >= 1e-6)."""
+        code = {"fp64": PRECISION_FP64, "fp32_grid": PRECISION_FP32_GRID}.get(precision, precision)
+        self.check(self.lib.se2p_plan_set_precision(self.handle, int(code)))
+        self.precision = "fp32_grid" if code == PRECISION_FP32_GRID else "fp64"
+
+    def set_overlap(self, on: bool = True):
+        self.check(self.lib.se2p_plan_set_overlap(self.handle, 1 if on else 0))
 
     def enable_timing(self, on: bool = True):
         self.check(self.lib.se2p_plan_enable_timing(self.handle, 1 if on else 0))

@@ -65,6 +65,8 @@ struct se2p_plan_st {
     int64_t launches = 0;
     DevBuf buf[S_COUNT_SLOTS];
     std::map<std::tuple<int, int, int, int>, cufftHandle> ffts;  // (Mx, My, batch, dir)
+    int precision = SE2P_PRECISION_FP64;
+    bool overlap = true;             // real space concurrent with the k-space chain
     bool timing = false;
     bool count_pairs = false;
     // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
@@ -247,6 +249,7 @@ int finish_out(se2p_plan pl, const OutBuf &o)
     return SE2P_OK;
 }
 
+// dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32)
 int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
 {
     auto key = std::make_tuple(Mx, My, batch, dir);
@@ -259,10 +262,12 @@ int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
     int n[2] = {Mx, My};
     const int real_dist = Mx * My, cplx_dist = Mx * (My / 2 + 1);
     cufftHandle p;
-    if (dir == 0)
-        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, CUFFT_D2Z, batch));
+    const bool fwd = dir == 0 || dir == 2;
+    const cufftType type = dir == 0 ? CUFFT_D2Z : dir == 1 ? CUFFT_Z2D : dir == 2 ? CUFFT_R2C : CUFFT_C2R;
+    if (fwd)
+        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, type, batch));
     else
-        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, CUFFT_Z2D, batch));
+        CKF(cufftPlanMany(&p, 2, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, type, batch));
     CKF(cufftSetStream(p, pl->stream));
     pl->ffts[key] = p;
     *h = p;
@@ -464,19 +469,73 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             ra.counters = static_cast<unsigned long long *>(pl->buf[S_COUNTERS].p);
         }
         // Real space on the side stream, overlapping the k-space chain.
-        cudaStream_t rs = J.kspace ? pl->side : st;
-        if (J.kspace) {
+        const bool side = J.kspace && pl->overlap;
+        cudaStream_t rs = side ? pl->side : st;
+        if (side) {
             CK(cudaEventRecord(pl->fork, st));
             CK(cudaStreamWaitEvent(rs, pl->fork, 0));
         }
         {
             StageTimer tm(pl, T_REAL, rs);
-            CK(launch_real(ra, J.slp, J.dlp, rs, pl->launches));
+            CK(launch_real(ra, J.slp, J.dlp, rs, pl->launches,
+                           pl->precision == SE2P_PRECISION_FP32_GRID));
         }
-        if (J.kspace) CK(cudaEventRecord(pl->join, rs));
+        if (side) CK(cudaEventRecord(pl->join, rs));
     }
 
-    if (J.kspace) {
+    if (J.kspace && pl->precision == SE2P_PRECISION_FP32_GRID) {
+        // FP32-grid form: spread, FFT, filter and gather in FP32 (se2p_kernels_f32.cu)
+        const int Mx = J.Mx, My = J.My, P = J.P;
+        const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
+        const int nout = (J.slp ? 2 : 0) + (J.dlp ? 2 : 0);
+        const double h = J.Lx / Mx;
+        float *grid = nullptr;
+        cufftComplex *spec = nullptr;
+        CKS(ensure_t(pl, S_GRID, G * nc, &grid));
+        CKS(ensure_t(pl, S_SPEC, H * nc, &spec));
+        CKS(ensure_t(pl, S_UK, ntz * (nout / 2), &uk));
+        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G * nc, st));
+        SpreadArgsF sa{sp, coef, ns, grid, Mx, My, P, J.Lx / 2.0, J.Ly / 2.0, h, J.w,
+                       -2 * J.xi * J.xi / J.eta};
+        {
+            StageTimer tm(pl, T_SPREAD);
+            CK(launch_spread_f32(sa, nc, sm_count(), st, pl->launches));
+        }
+        cufftHandle fwd, inv;
+        CKS(get_fft(pl, Mx, My, nc, 2, &fwd));
+        {
+            StageTimer tm(pl, T_FFT_FWD);
+            CKF(cufftExecR2C(fwd, grid, spec));
+        }
+        FilterArgsF fa;
+        fa.spec = reinterpret_cast<float2 *>(spec);
+        fa.Mx = Mx;
+        fa.My = My;
+        fa.Lx = J.Lx;
+        fa.Ly = J.Ly;
+        fa.xi = J.xi;
+        fa.eta = J.eta;
+        fa.scale = (float)(1.0 / ((double)Mx * (double)My));
+        fa.slp_in = J.slp ? 0 : -1;
+        fa.dlp_in = J.dlp ? doff : -1;
+        fa.slp_out = 0;
+        fa.dlp_out = J.slp ? 2 : 0;
+        {
+            StageTimer tm(pl, T_FILTER);
+            CK(launch_filter_f32(fa, st, pl->launches));
+        }
+        CKS(get_fft(pl, Mx, My, nout, 3, &inv));
+        {
+            StageTimer tm(pl, T_FFT_INV);
+            CKF(cufftExecC2R(inv, spec, grid));
+        }
+        double s = 4 * J.xi * J.xi / J.eta;               // mex_stokes_slp_kspace.cpp:325-328
+        s = s * s * h * h / kPi;
+        GatherArgsF ga{tp, nt, grid, Mx, My, P, J.Lx / 2.0, J.Ly / 2.0, h, J.w,
+                       -2 * J.xi * J.xi / J.eta, s / (4 * kPi), uk};
+        StageTimer tm(pl, T_GATHER);
+        CK(launch_gather_f32(ga, nout, st, pl->launches));
+    } else if (J.kspace) {
         const int Mx = J.Mx, My = J.My, P = J.P;
         const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
         const int nout = (J.slp ? 2 : 0) + (J.dlp ? 2 : 0);
@@ -575,7 +634,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         CK(launch_zero_mode(ns, ps, fd, nr, 1.0 / (J.Lx * J.Ly), part, zm, st, pl->launches));
     }
 
-    if (J.real && J.kspace) CK(cudaStreamWaitEvent(st, pl->join, 0));
+    if (J.real && J.kspace && pl->overlap) CK(cudaStreamWaitEvent(st, pl->join, 0));
     StageTimer *t_asm = new StageTimer(pl, T_ASSEMBLE);
     const double2 *uk_slp = (J.kspace && J.slp) ? uk : nullptr;
     const double2 *uk_dlp = (J.kspace && J.dlp) ? uk + (J.slp ? nt : 0) : nullptr;
@@ -689,6 +748,22 @@ int se2p_plan_enable_timing(se2p_plan pl, int on)
 }
 
 int se2p_num_stages(void) { return T_NUM_STAGES; }
+
+int se2p_plan_set_overlap(se2p_plan pl, int on)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    pl->overlap = on != 0;
+    return SE2P_OK;
+}
+
+int se2p_plan_set_precision(se2p_plan pl, int precision)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    if (precision != SE2P_PRECISION_FP64 && precision != SE2P_PRECISION_FP32_GRID)
+        return fail(pl, SE2P_ERR_ARG, "unknown precision %d", precision);
+    pl->precision = precision;
+    return SE2P_OK;
+}
 
 int se2p_plan_count_pairs(se2p_plan pl, int on, int64_t *counts, int reset)
 {

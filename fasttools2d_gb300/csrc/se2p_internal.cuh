@@ -176,6 +176,33 @@ struct GatherArgs {
     double2 *out;         // NC/2 outputs per target, [k * nt + t]
 };
 
+// FP32-grid (mixed precision) k-space arguments (se2p_kernels_f32.cu).
+struct SpreadArgsF {
+    const double2 *sp;
+    const double *coef;
+    int64_t ns;
+    float *grid;
+    int Mx, My, P;
+    double Lhx, Lhy, h, w, a;
+};
+
+struct FilterArgsF {
+    float2 *spec;
+    int Mx, My;
+    double Lx, Ly, xi, eta;
+    float scale;
+    int slp_in, dlp_in, slp_out, dlp_out;
+};
+
+struct GatherArgsF {
+    const double2 *tp;
+    int64_t nt;
+    const float *grid;
+    int Mx, My, P;
+    double Lhx, Lhy, h, w, a, scale;
+    double2 *out;
+};
+
 // ---------------------------------------------------------------------------
 // Host launchers (se2p_kernels.cu).  Each returns the launch status.
 // ---------------------------------------------------------------------------
@@ -186,7 +213,12 @@ cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
                             const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
                             cudaStream_t st, int64_t &launches);
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                        int64_t &launches);
+                        int64_t &launches, bool mixed = false);
+int sm_count();
+cudaError_t launch_spread_f32(const SpreadArgsF &a, int nc, int sms, cudaStream_t st,
+                              int64_t &launches);
+cudaError_t launch_filter_f32(const FilterArgsF &a, cudaStream_t st, int64_t &launches);
+cudaError_t launch_gather_f32(const GatherArgsF &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches);

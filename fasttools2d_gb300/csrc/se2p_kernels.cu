@@ -381,23 +381,106 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
     }
 }
 
+// The E1 Pade sets in FP32, same layout as c_e1.
+__constant__ float c_e1f[3][22] = {
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+     -17.70313744792479226930481672752649f, -2.03222164752550948918496942496859f,
+     -9.56230625623594754358691716333851f, 24.24775264986217493401454703416675f,
+     -0.99999982131078080094255255971802f, 34.82867640350680460414878325536847f,
+     -0.00000000083503088648841284312372f, 11.56228921223568129050818242831156f},
+    {-1185.45720315201027667f, -0.776491285282330997549f, -14751.4895786128450662f,
+     1229.20784182403048905f, -54844.4587226402067411f, 18455.4124737722049515f,
+     -86273.1567711649528784f, 86722.3403467334749201f, -66598.2652345418633509f,
+     180329.498380501819718f, -27182.6254466733970467f, 192104.047790227984431f,
+     -6046.8250112711035463f, 113057.05869159631492f, -724.581482791462469795f,
+     38129.5594484818471461f, -43.3058660811817946037f, 7417.37624454689546708f,
+     -0.999999999999998811143f, 809.193214954550328455f, -0.121013190657725568138e-18f,
+     45.3058660811801465927f},
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+     -0.000111507792921197858394f, -0.528611029520217142048e-6f,
+     -0.00399167106081113256961f, 0.000131049900798434683324f,
+     -0.0368031736257943745142f, 0.00427347600017103698101f,
+     -0.245088216639761496153f, 0.056770677104207528384f,
+     0.0320913665303559189999f, 0.37091387659397013215f,
+     0.0865197248079397976498f, 1.0f}};
+
+// A pair in FP32 (mixed-precision form, far pairs): the offsets are formed in
+// FP64 in each kernel's own order, then everything runs in FP32.
+template <bool SLP, bool DLP>
+__device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp &W, int2 e,
+                                              const float *e1f, float &s1, float &s2, float &d1,
+                                              float &d2)
+{
+    const int s = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
+    const double2 S = a.sp[s];
+    const double2 T = W.tpos[slot];
+    const int tb = W.tbox[slot];
+    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    const float x1 = (float)((S.x - T.x) + zx), x2 = (float)((S.y - T.y) + zy);
+    const float dxs = (float)(S.x - (T.x - zx)), dys = (float)(S.y - (T.y - zy));
+    const float xi2 = a.xi2f;
+    if (SLP && (fl & 1)) {
+        const float r2 = fmaf(dxs, dxs, dys * dys);
+        const float x = r2 * xi2;
+        const float ex = __expf(-x);
+        const float ir2 = 1.0f / r2;
+        const int set = x >= 16.f ? 0 : (x > 1.f ? 1 : 2);
+        const float *c = e1f + 22 * set;
+        const float z = set == 2 ? x : ir2 * (float)a.inv_xi2;
+        float pa = c[0], pb = c[1];
+#pragma unroll
+        for (int i = 2; i < 22; i += 2) {
+            pa = fmaf(z, pa, c[i]);
+            pb = fmaf(z, pb, c[i + 1]);
+        }
+        const float E = set == 2 ? pa / pb + x - __logf(x) - 0.66373538970947265625f
+                                 : ex * (z + pa / (pb + x));
+        const float f1 = (float)a.coef[(int64_t)a.nc * s], f2 = (float)a.coef[(int64_t)a.nc * s + 1];
+        const float h = 0.5f * E, gq = ex * ir2 * fmaf(dxs, f2, -dys * f1);
+        s1 = fmaf(h, f1, fmaf(gq, dys, s1));
+        s2 = fmaf(h, f2, fmaf(-gq, dxs, s2));
+    }
+    if (DLP && (fl & 2)) {
+        const double *Sc = a.coef + (int64_t)a.nc * s + a.doff;
+        const float S11 = (float)Sc[0], S1221 = (float)Sc[1], S22 = (float)Sc[2];
+        const float r2 = fmaf(x1, x1, x2 * x2);
+        const float x = r2 * xi2;
+        const float ex = __expf(-x);
+        const float ir2 = 1.0f / r2;
+        const float fb = -4.f * (1.f + x) * ir2 * ir2;
+        const float Q = fmaf(x1 * x1, S11, fmaf(x1 * x2, S1221, x2 * x2 * S22));
+        const float A1 = fmaf(x1, fmaf(3.f, S11, S22), x2 * S1221);
+        const float A2 = fmaf(x2, fmaf(3.f, S22, S11), x1 * S1221);
+        const float fq = fb * Q, pf = 2.f * xi2;
+        d1 = fmaf(ex, fmaf(fq, x1, pf * A1), d1);
+        d2 = fmaf(ex, fmaf(fq, x2, pf * A2), d2);
+    }
+}
+
 // Lane-side state of one pair FIFO.
 struct PairQueue {
     int qn;               // entries queued (warp-uniform)
     long long enq, proc;  // entries enqueued / processed so far (warp-uniform)
     int tag;              // sequence number of the target this lane's sums belong to
     double s1, s2, d1, d2;
+    float f1, f2, g1, g2; // FP32 sums of the mixed-precision form
 };
 
-template <bool SLP, bool DLP>
+template <bool SLP, bool DLP, bool MIXED>
 __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
 {
     __shared__ RealWarp warps[kRealWarps];
     __shared__ double tab[64];
     __shared__ double e1s[66];
+    __shared__ float e1f[66];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
-    for (int i = threadIdx.x; i < 66; i += blockDim.x) e1s[i] = (&c_e1[0][0])[i];
+    for (int i = threadIdx.x; i < 66; i += blockDim.x) {
+        e1s[i] = (&c_e1[0][0])[i];
+        e1f[i] = (&c_e1f[0][0])[i];
+    }
     __syncthreads();
     RealWarp &W = warps[wid];
     const int64_t nw = (int64_t)gridDim.x * kRealWarps;
@@ -408,6 +491,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
     for (int j = 0; j < 2; j++) {
         Q[j].qn = 0; Q[j].enq = 0; Q[j].proc = 0; Q[j].tag = -1;
         Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
+        Q[j].f1 = Q[j].f2 = Q[j].g1 = Q[j].g2 = 0.f;
     }
     unsigned long long ncand = 0, nslp = 0, ndlp = 0;
 
@@ -423,16 +507,20 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         int eseq = -1;
         if (e.y >= 0) eseq = gseq - nfl + (((e.y & 0xff) - head + kRing) % kRing);
         const bool fl = P.tag >= 0 && (lane >= cnt || P.tag != eseq);
+        const bool f32 = MIXED && j == 0;
         if (__any_sync(~0u, fl)) {
-            seg_flush(W, lane, P.tag, fl ? P.s1 : 0.0, fl ? P.s2 : 0.0, fl ? P.d1 : 0.0,
-                      fl ? P.d2 : 0.0);
+            const double v0 = f32 ? (double)P.f1 : P.s1, v1 = f32 ? (double)P.f2 : P.s2;
+            const double v2 = f32 ? (double)P.g1 : P.d1, v3 = f32 ? (double)P.g2 : P.d2;
+            seg_flush(W, lane, P.tag, fl ? v0 : 0.0, fl ? v1 : 0.0, fl ? v2 : 0.0, fl ? v3 : 0.0);
             if (fl) {
                 P.s1 = P.s2 = P.d1 = P.d2 = 0.0;
+                P.f1 = P.f2 = P.g1 = P.g2 = 0.f;
                 P.tag = -1;
             }
         }
         if (lane < cnt) {
-            real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
+            if (f32) real_pair_f32<SLP, DLP>(a, W, e, e1f, P.f1, P.f2, P.g1, P.g2);
+            else real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
             P.tag = eseq;
         }
     };
@@ -455,8 +543,13 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         for (int j = 0; j < 2; j++) {
             batch(j, Q[j].qn);
             const int key = Q[j].tag >= 0 ? Q[j].tag : 0x7fffffff;
-            seg_flush(W, lane, key, Q[j].s1, Q[j].s2, Q[j].d1, Q[j].d2);
+            if (MIXED && j == 0)
+                seg_flush(W, lane, key, (double)Q[j].f1, (double)Q[j].f2, (double)Q[j].g1,
+                          (double)Q[j].g2);
+            else
+                seg_flush(W, lane, key, Q[j].s1, Q[j].s2, Q[j].d1, Q[j].d2);
             Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
+            Q[j].f1 = Q[j].f2 = Q[j].g1 = Q[j].g2 = 0.f;
             Q[j].tag = -1;
         }
         retire(true);
@@ -586,9 +679,12 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
     }
 }
 
-template __global__ void k_real<true, false>(RealArgs);
-template __global__ void k_real<false, true>(RealArgs);
-template __global__ void k_real<true, true>(RealArgs);
+template __global__ void k_real<true, false, false>(RealArgs);
+template __global__ void k_real<false, true, false>(RealArgs);
+template __global__ void k_real<true, true, false>(RealArgs);
+template __global__ void k_real<true, false, true>(RealArgs);
+template __global__ void k_real<false, true, true>(RealArgs);
+template __global__ void k_real<true, true, true>(RealArgs);
 
 // ===========================================================================
 // Gaussian spread (fast Gaussian gridding; PE/src/mex/StokesSLP/
@@ -998,7 +1094,7 @@ static inline unsigned grid_for(int64_t n, int block)
 }
 
 // Number of SMs of the current device (cached per process for device 0..63).
-static int sm_count()
+int sm_count()
 {
     static int cache[64] = {0};
     int dev = 0;
@@ -1044,15 +1140,21 @@ cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
 }
 
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                        int64_t &launches)
+                        int64_t &launches, bool mixed)
 {
     if (a.ntar <= 0) return cudaSuccess;
     const int64_t want = (a.ntar + kRealWarps - 1) / kRealWarps;
     const int64_t cap = (int64_t)sm_count() * 8;
     const unsigned g = (unsigned)(want < cap ? want : cap);
-    if (slp && dlp) k_real<true, true><<<g, kRealWarps * 32, 0, st>>>(a);
-    else if (slp) k_real<true, false><<<g, kRealWarps * 32, 0, st>>>(a);
-    else k_real<false, true><<<g, kRealWarps * 32, 0, st>>>(a);
+    if (mixed) {
+        if (slp && dlp) k_real<true, true, true><<<g, kRealWarps * 32, 0, st>>>(a);
+        else if (slp) k_real<true, false, true><<<g, kRealWarps * 32, 0, st>>>(a);
+        else k_real<false, true, true><<<g, kRealWarps * 32, 0, st>>>(a);
+    } else {
+        if (slp && dlp) k_real<true, true, false><<<g, kRealWarps * 32, 0, st>>>(a);
+        else if (slp) k_real<true, false, false><<<g, kRealWarps * 32, 0, st>>>(a);
+        else k_real<false, true, false><<<g, kRealWarps * 32, 0, st>>>(a);
+    }
     launches++;
     return cudaGetLastError();
 }

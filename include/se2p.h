@@ -61,11 +61,27 @@ int se2p_plan_destroy(se2p_plan plan);
  * uses a private non-blocking stream. */
 int se2p_plan_set_stream(se2p_plan plan, void *cuda_stream);
 const char *se2p_plan_last_error(se2p_plan plan);
+/* Real space runs on a plan-owned side stream, concurrently with the k-space
+ * chain, unless overlap is switched off (on = 0): then every stage runs in
+ * order on the plan's stream, e.g. to time kernels in isolation. */
+int se2p_plan_set_overlap(se2p_plan plan, int on);
 /* Bytes of device workspace the plan currently holds. */
 int64_t se2p_plan_workspace_bytes(se2p_plan plan);
 /* Number of kernels this plan has launched so far (its own, not cuFFT's). */
 int64_t se2p_plan_kernel_launches(se2p_plan plan);
 const char *se2p_version(void);
+
+/* ---- precision ----------------------------------------------------------------
+ * SE2P_PRECISION_FP64 (default): every step in FP64, matching the reference
+ * to <= 1e-12.  SE2P_PRECISION_FP32_GRID: the mixed form for tolerances
+ * >= 1e-6 -- spreading, FFT, filter and gather in FP32 and the far real-space
+ * pairs (xi^2 r^2 > 1) in FP32, while the near real-space pairs (E1 at small
+ * argument), the SLP self term and the DLP k=0 term stay FP64; the pair set,
+ * box assignment and stencil origins stay exactly the reference's.  No
+ * reference counterpart (the reference is FP64 only).  Applies to all later
+ * calls on the plan. */
+typedef enum { SE2P_PRECISION_FP64 = 0, SE2P_PRECISION_FP32_GRID = 1 } se2p_precision;
+int se2p_plan_set_precision(se2p_plan plan, int precision);
 
 /* ---- stage timing ------------------------------------------------------------
  * Replaces the drivers' `verbose` tic/toc prints (StokesSLP_ewald_2p.m:106-131):

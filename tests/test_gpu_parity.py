@@ -128,7 +128,7 @@ def test_repeatable(ft, plan):
     prm = ft.EwaldParams.derived(40.0, 8, 8, 128, 128, 24, 1.0, 1.0)
     a = ft.stokes_ewald(p, p, f, g, n, prm, plan=plan)
     b = ft.stokes_ewald(p, p, f, g, n, prm, plan=plan)
-    assert relerr(a[0], b[0]) < 1e-14 and relerr(a[1], b[1]) < 1e-14
+    assert relerr(a[0], b[0]) < 1e-13 and relerr(a[1], b[1]) < 1e-13
 
 
 def test_linearity_in_forces(ft, plan):
