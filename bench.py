@@ -285,6 +285,81 @@ def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
             "error_vs_fp64": err}
 
 
+# Config 5: forward + adjoint, N = 2^18.
+N5, XI5, RC5, M5, P5 = 2 ** 18, 430.0, 0.011, 1344, 24
+
+
+def adjoint_leg(plan, steps, timed, dev):
+    """Config 5: time of the forward and of forward + adjoint (gradients of
+    J = sum_t w_slp.u_slp + w_dlp.u_dlp w.r.t. source positions, forces,
+    densities, normals), and a central-difference check of the gradients on
+    16 random coordinates (h = 1e-6, J from the GPU forward)."""
+    import torch
+    import fasttools2d_gb300 as ft
+    rng = np.random.default_rng(20261203 + 5)
+    N = N5
+    arrs = [rng.random((N, 2)), rng.random((N, 2)), rng.standard_normal((N, 2)),
+            rng.standard_normal((N, 2))]
+    th = rng.random(N) * 2 * np.pi
+    arrs.append(np.stack([np.cos(th), np.sin(th)], axis=1))
+    w = [rng.standard_normal((N, 2)), rng.standard_normal((N, 2))]
+    T = [torch.from_numpy(a).to(dev) for a in arrs]
+    Wt = [torch.from_numpy(a).to(dev) for a in w]
+    nside = int(math.floor(L / RC5))
+    prm = ft.EwaldParams.derived(XI5, nside, nside, M5, M5, P5, L, L)
+    c = prm.as_c()
+    Lb = plan.lib
+    u = [torch.empty((N, 2), dtype=torch.float64, device=dev) for _ in range(2)]
+    g = [torch.empty((N, 2), dtype=torch.float64, device=dev) for _ in range(4)]
+
+    def fwd():
+        plan.check(Lb.se2p_stokes_ewald(plan.handle, ctypes.byref(c), T[0].data_ptr(), N,
+                                        T[1].data_ptr(), N, T[2].data_ptr(), T[3].data_ptr(),
+                                        T[4].data_ptr(), u[0].data_ptr(), u[1].data_ptr()))
+
+    def adj():
+        plan.check(Lb.se2p_stokes_ewald_adjoint(
+            plan.handle, ctypes.byref(c), T[0].data_ptr(), N, T[1].data_ptr(), N,
+            T[2].data_ptr(), T[3].data_ptr(), T[4].data_ptr(), Wt[0].data_ptr(),
+            Wt[1].data_ptr(), g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+            g[3].data_ptr()))
+
+    def both():
+        fwd()
+        adj()
+    for _ in range(3):
+        both()
+    t_f = timed(fwd, steps) / steps
+    t_fa = timed(both, steps) / steps
+    # finite differences on 16 coordinates: positions, forces, densities, normals
+    both()
+    torch.cuda.synchronize(dev)
+    G = [x.cpu().numpy() for x in g]
+    pick = np.random.default_rng(1)
+    worst = 0.0
+    h = 1e-6
+    which = {0: 0, 2: 1, 3: 2, 4: 3}          # input array -> gradient array
+
+    def J():
+        fwd()
+        return float((Wt[0] * u[0]).sum() + (Wt[1] * u[1]).sum())
+    for _ in range(16):
+        a = int(pick.choice([0, 2, 3, 4]))
+        i, k = int(pick.integers(0, N)), int(pick.integers(0, 2))
+        x0 = float(T[a][i, k])
+        T[a][i, k] = x0 + h
+        jp = J()
+        T[a][i, k] = x0 - h
+        jm = J()
+        T[a][i, k] = x0
+        gi = G[which[a]]
+        worst = max(worst, abs((jp - jm) / (2 * h) - gi[i, k]) / np.abs(gi).max())
+    return {"workload": f"config 5: N={N} sources + {N} targets uniform, xi={XI5}, rc={RC5} "
+                        f"(nside={nside}), M={M5}, P={P5}, FP64; J = sum_t w.u with w ~ N(0,1)",
+            "fwd_ms": t_f, "fwd_adjoint_ms": t_fa, "ratio_fwd_adjoint_over_fwd": t_fa / t_f,
+            "fd_check": {"coords": 16, "h": h, "max_err_rel_to_max_grad": worst}}
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -397,6 +472,7 @@ def gpu_arm(args, rank, world, local_rank):
 
     # ---- FP32-grid form (config 4) next to the FP64 form on the same workload
     mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev)
+    adjoint = adjoint_leg(plan, args.steps, timed, dev)
 
     # ---- roofline of the dominant kernel ---------------------------------
     kstages = {k: v for k, v in stages.items() if k not in ("h2d", "d2h") and v[1] > 0}
@@ -426,7 +502,7 @@ def gpu_arm(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config(N, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
         "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
-        "clocks": clk.summary(), "fp32_grid": mixed,
+        "clocks": clk.summary(), "fp32_grid": mixed, "adjoint": adjoint,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N)

@@ -26,7 +26,7 @@ EXPORTS = (
     "se2p_slp_ewald", "se2p_dlp_ewald", "se2p_stokes_ewald",
     "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
     "se2p_plan_count_pairs", "se2p_slp_real_noalloc", "se2p_plan_set_precision",
-    "se2p_plan_set_overlap",
+    "se2p_plan_set_overlap", "se2p_stokes_ewald_adjoint",
 )
 PRECISION_FP64, PRECISION_FP32_GRID = 0, 1
 
@@ -89,6 +89,8 @@ def load(path: str = LIB_PATH):
         L.se2p_slp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp]
         L.se2p_dlp_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp]
         L.se2p_stokes_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp]
+        L.se2p_stokes_ewald_adjoint.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp,
+                                                _dp, _dp, _dp, _dp]
         for name in EXPORTS:
             if name not in ("se2p_version",):
                 getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int

@@ -36,6 +36,7 @@ enum Slot {
     S_UR_SLP, S_UR_DLP, S_UK,                   // partial results (sorted order)
     S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM, S_COUNTERS,
     S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
+    S_IN_W1, S_IN_W2, S_WCOEF, S_GR, S_GK, S_SBOXS, S_ZEROS,   // adjoint
     S_COUNT_SLOTS
 };
 
@@ -659,6 +660,241 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     return SE2P_OK;
 }
 
+// --------------------------------------------------------------------------
+// Adjoint: gradients of J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t), with
+// u_slp, u_dlp exactly as se2p_stokes_ewald returns them, with respect to the
+// (unwrapped) source positions, SLP forces, DLP densities and normals.
+// --------------------------------------------------------------------------
+struct AdjIo {
+    const double *psrc, *ptar, *f_slp, *f_dlp, *nrm, *w_slp, *w_dlp;
+    int64_t ns, nt;
+    double *g_pos, *g_fs, *g_fd, *g_n;
+};
+
+int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
+{
+    DeviceGuard guard(pl->device);
+    cudaStream_t st = pl->stream;
+    bool host_io = false;
+    const int64_t ns = io.ns, nt = io.nt;
+    const bool slp = J.slp, dlp = J.dlp;
+    const double2 *ps, *pt, *fs = nullptr, *fd = nullptr, *nr = nullptr, *w1 = nullptr, *w2 = nullptr;
+    CKS(stage_in(pl, S_IN_PS, io.psrc, ns, &ps, &host_io));
+    CKS(stage_in(pl, S_IN_PT, io.ptar, nt, &pt, &host_io));
+    if (slp) {
+        CKS(stage_in(pl, S_IN_F, io.f_slp, ns, &fs, &host_io));
+        CKS(stage_in(pl, S_IN_W1, io.w_slp, nt, &w1, &host_io));
+    }
+    if (dlp) {
+        CKS(stage_in(pl, S_IN_FD, io.f_dlp, ns, &fd, &host_io));
+        CKS(stage_in(pl, S_IN_N, io.nrm, ns, &nr, &host_io));
+        CKS(stage_in(pl, S_IN_W2, io.w_dlp, nt, &w2, &host_io));
+    }
+    OutBuf o_p, o_fs, o_fd, o_n;
+    CKS(stage_out(pl, S_OUT0, io.g_pos, ns, &o_p, &host_io));
+    CKS(stage_out(pl, S_OUT1, slp ? io.g_fs : nullptr, ns, &o_fs, &host_io));
+    CKS(stage_out(pl, S_OUT2, dlp ? io.g_fd : nullptr, ns, &o_fd, &host_io));
+    CKS(stage_out(pl, S_OUT3, dlp ? io.g_n : nullptr, ns, &o_n, &host_io));
+    if (ns == 0) return SE2P_OK;
+
+    const size_t nsz = (size_t)ns, ntz = (size_t)(nt > 0 ? nt : 1);
+    double2 *ws = nullptr, *wt = nullptr;
+    CKS(ensure_t(pl, S_WPS, nsz, &ws));
+    CKS(ensure_t(pl, S_WPT, ntz, &wt));
+    CK(launch_wrap(ns, ps, J.Lx, J.Ly, ws, st, pl->launches));
+    CK(launch_wrap(nt, pt, J.Lx, J.Ly, wt, st, pl->launches));
+
+    const int nx = J.nx, ny = J.ny, nbox = nx * ny;
+    int *sbox, *srank, *tbox, *trank, *count, *sstart, *tstart, *sperm, *tperm, *tboxs, *sboxs;
+    double2 *sp, *tp;
+    float2 *spf, *tpf;
+    CKS(ensure_t(pl, S_SBOX, nsz, &sbox));
+    CKS(ensure_t(pl, S_SRANK, nsz, &srank));
+    CKS(ensure_t(pl, S_TBOX, ntz, &tbox));
+    CKS(ensure_t(pl, S_TRANK, ntz, &trank));
+    CKS(ensure_t(pl, S_COUNT, (size_t)nbox, &count));
+    CKS(ensure_t(pl, S_SSTART, (size_t)nbox + 1, &sstart));
+    CKS(ensure_t(pl, S_TSTART, (size_t)nbox + 1, &tstart));
+    CKS(ensure_t(pl, S_SPERM, nsz, &sperm));
+    CKS(ensure_t(pl, S_TPERM, ntz, &tperm));
+    CKS(ensure_t(pl, S_TBOXS, ntz, &tboxs));
+    CKS(ensure_t(pl, S_SBOXS, nsz, &sboxs));
+    CKS(ensure_t(pl, S_SP, nsz, &sp));
+    CKS(ensure_t(pl, S_TP, ntz, &tp));
+    CKS(ensure_t(pl, S_SPF, nsz, &spf));
+    CKS(ensure_t(pl, S_TPF, ntz, &tpf));
+    {
+        StageTimer tm(pl, T_SORT);
+        BinArgs bs{ws, ns, J.Lx, J.Ly, nx, ny, sbox, srank, count};
+        CK(launch_bin(bs, sstart, nbox, sperm, sboxs, sp, spf, st, pl->launches));
+        BinArgs bt{wt, nt, J.Lx, J.Ly, nx, ny, tbox, trank, count};
+        CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, tpf, st, pl->launches));
+    }
+    // 5 coefficients per sorted source (absent kinds as zeros) and the
+    // targets' weights (w_slp, w_dlp) in sorted order.
+    double *coef = nullptr, *wcoef = nullptr;
+    double2 *zeros = nullptr;
+    CKS(ensure_t(pl, S_COEF, 5 * nsz, &coef));
+    CKS(ensure_t(pl, S_WCOEF, 4 * ntz, &wcoef));
+    CKS(ensure_t(pl, S_ZEROS, nsz, &zeros));
+    CK(cudaMemsetAsync(zeros, 0, sizeof(double2) * nsz, st));
+    {
+        StageTimer tm(pl, T_COEF);
+        CK(launch_src_coef(ns, sperm, slp ? fs : zeros, dlp ? fd : zeros, dlp ? nr : zeros, coef, 5,
+                           st, pl->launches));
+        CK(launch_sorted_pair(nt, tperm, w1, w2, wcoef, st, pl->launches));
+    }
+    double *gr = nullptr, *gk = nullptr;
+    CKS(ensure_t(pl, S_GR, 7 * nsz, &gr));
+    CKS(ensure_t(pl, S_GK, 7 * nsz, &gk));
+
+    // real space (side stream) ...
+    RealArgs ra;
+    memset(&ra, 0, sizeof ra);
+    ra.sp = sp;
+    ra.spf = spf;
+    ra.coef = coef;
+    ra.nc = 5;
+    ra.doff = 2;
+    ra.sstart = tstart;            // candidate (inner) cell list: the targets
+    ra.tp = tp;
+    ra.tpf = tpf;
+    ra.tbox = tboxs;
+    ra.ntar = nt;
+    ra.nx = nx;
+    ra.ny = ny;
+    ra.Lx = J.Lx;
+    ra.Ly = J.Ly;
+    ra.xi = J.xi;
+    ra.xi2 = J.xi * J.xi;
+    ra.cut2 = J.Lx * J.Ly / nx / ny;
+    ra.cut2f = (float)ra.cut2;
+    ra.xi2f = (float)(J.xi * J.xi);
+    ra.inv_xi2 = 1.0 / (J.xi * J.xi);
+    ra.pf = 2.0 * J.xi * J.xi;
+    ra.zxm = (J.Lx * (double)(-nx)) / nx;
+    ra.zxp = (J.Lx * (double)nx) / nx;
+    ra.zym = (J.Ly * (double)(-ny)) / ny;
+    ra.zyp = (J.Ly * (double)ny) / ny;
+    ra.self_c = -1.288607832450766155 - std::log(J.xi);
+    ra.nouter = ns;
+    ra.obox = sboxs;
+    ra.wcoef = wcoef;
+    ra.gout = gr;
+    const bool side = pl->overlap;
+    cudaStream_t rs = side ? pl->side : st;
+    if (side) {
+        CK(cudaEventRecord(pl->fork, st));
+        CK(cudaStreamWaitEvent(rs, pl->fork, 0));
+    }
+    {
+        StageTimer tm(pl, T_REAL, rs);
+        CK(launch_real_adj(ra, slp, dlp, rs, pl->launches));
+    }
+    if (side) CK(cudaEventRecord(pl->join, rs));
+
+    // ... k space: spread w at the targets, D2Z, adjoint filter, Z2D, gather
+    // with weight gradients at the sources.
+    const int Mx = J.Mx, My = J.My, P = J.P;
+    const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
+    const double h = J.Lx / Mx;
+    double *grid = nullptr, *e1 = nullptr;
+    cufftDoubleComplex *spec = nullptr;
+    CKS(ensure_t(pl, S_GRID, G * 5, &grid));
+    CKS(ensure_t(pl, S_SPEC, H * 5, &spec));
+    CKS(ensure_t(pl, S_E1, (size_t)P + 1, &e1));
+    double e1h[kMaxP + 1];
+    const double t = -2 * J.xi * J.xi / J.eta * h * h;
+    for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
+    CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * 4, st));
+    SpreadArgs sa;
+    sa.sp = tp;
+    sa.coef = wcoef;
+    sa.ns = nt;
+    sa.grid = grid;
+    sa.Mx = Mx;
+    sa.My = My;
+    sa.P = P;
+    sa.Lhx = J.Lx / 2.0;
+    sa.Lhy = J.Ly / 2.0;
+    sa.h = h;
+    sa.w = J.w;
+    sa.a = -2 * J.xi * J.xi / J.eta;
+    sa.e1 = e1;
+    {
+        StageTimer tm(pl, T_SPREAD);
+        CK(launch_spread(sa, 4, st, pl->launches));
+    }
+    cufftHandle fwd, inv;
+    CKS(get_fft(pl, Mx, My, 4, 0, &fwd));
+    {
+        StageTimer tm(pl, T_FFT_FWD);
+        CKF(cufftExecD2Z(fwd, grid, spec));
+    }
+    FilterArgs fa;
+    fa.spec = spec;
+    fa.Mx = Mx;
+    fa.My = My;
+    fa.Lx = J.Lx;
+    fa.Ly = J.Ly;
+    fa.xi = J.xi;
+    fa.eta = J.eta;
+    fa.scale = 1.0 / ((double)Mx * (double)My);
+    fa.slp_in = 0;
+    fa.slp_out = 0;
+    fa.dlp_in = 2;
+    fa.dlp_out = 2;
+    {
+        StageTimer tm(pl, T_FILTER);
+        CK(launch_filter_adj(fa, st, pl->launches));
+    }
+    CKS(get_fft(pl, Mx, My, 5, 1, &inv));
+    {
+        StageTimer tm(pl, T_FFT_INV);
+        CKF(cufftExecZ2D(inv, spec, grid));
+    }
+    GatherAdjArgs ga;
+    ga.sp = sp;
+    ga.ns = ns;
+    ga.coef = coef;
+    ga.grid = grid;
+    ga.Mx = Mx;
+    ga.My = My;
+    ga.P = P;
+    ga.Lhx = J.Lx / 2.0;
+    ga.Lhy = J.Ly / 2.0;
+    ga.h = h;
+    ga.w = J.w;
+    ga.a = -2 * J.xi * J.xi / J.eta;
+    double sg = 4 * J.xi * J.xi / J.eta;
+    sg = sg * sg * h * h / kPi;
+    ga.scale = sg / (4 * kPi);
+    ga.e1 = e1;
+    ga.out = gk;
+    {
+        StageTimer tm(pl, T_GATHER);
+        CK(launch_gather_adj(ga, st, pl->launches));
+    }
+    if (side) CK(cudaStreamWaitEvent(st, pl->join, 0));
+
+    double2 *part = nullptr;
+    CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
+    {
+        StageTimer tm(pl, T_ASSEMBLE);
+        CK(launch_adj_assemble(ns, sperm, gr, gk, wcoef, nt, part, ps, dlp ? fd : zeros,
+                               dlp ? nr : zeros, 1.0 / (J.Lx * J.Ly), slp, dlp, o_p.dev,
+                               o_fs.dev, o_fd.dev, o_n.dev, st, pl->launches));
+    }
+    CKS(finish_out(pl, o_p));
+    CKS(finish_out(pl, o_fs));
+    CKS(finish_out(pl, o_fd));
+    CKS(finish_out(pl, o_n));
+    if (host_io) CK(cudaStreamSynchronize(st));
+    else CK(cudaGetLastError());
+    return SE2P_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -944,6 +1180,29 @@ int se2p_stokes_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, 
     io.ns = ns; io.nt = nt;
     io.u_slp = u_slp; io.u_dlp = u_dlp; io.mode_slp = 3; io.mode_dlp = 4;
     return run(pl, J, io);
+}
+
+int se2p_stokes_ewald_adjoint(se2p_plan pl, const se2p_params *prm, const double *psrc,
+                              int64_t ns, const double *ptar, int64_t nt, const double *f_slp,
+                              const double *f_dlp, const double *n, const double *w_slp,
+                              const double *w_dlp, double *g_psrc, double *g_fslp,
+                              double *g_fdlp, double *g_n)
+{
+    if (!pl) return SE2P_ERR_ARG;
+    CKS(check_params(pl, prm));
+    const bool slp = f_slp && w_slp, dlp = f_dlp && n && w_dlp;
+    if (!slp && !dlp) return fail(pl, SE2P_ERR_ARG, "neither SLP (f_slp, w_slp) nor DLP (f_dlp, n, w_dlp) given");
+    if (ns < 0 || nt < 0) return fail(pl, SE2P_ERR_ARG, "negative point count");
+    if (ns > 0x7fffffff || nt > 0x7fffffff) return fail(pl, SE2P_ERR_UNSUPPORTED, "more than 2^31-1 points");
+    if ((ns > 0 && !psrc) || (nt > 0 && !ptar)) return fail(pl, SE2P_ERR_ARG, "null point array");
+    if (!(std::isfinite(prm->xi) && prm->xi > 0 && prm->Lx > 0 && prm->Ly > 0))
+        return fail(pl, SE2P_ERR_ARG, "bad xi / box");
+    Job J;
+    job_from_params(J, prm);
+    J.slp = slp;
+    J.dlp = dlp;
+    AdjIo io{psrc, ptar, f_slp, f_dlp, n, w_slp, w_dlp, ns, nt, g_psrc, g_fslp, g_fdlp, g_n};
+    return run_adjoint(pl, J, io);
 }
 
 }  // extern "C"

@@ -146,6 +146,25 @@ struct RealArgs {
     double2 *u_slp;       // raw sums per sorted target (no 1/(4 pi))
     double2 *u_dlp;
     unsigned long long *counters;   // [candidates, SLP pairs, DLP pairs] (may be NULL)
+    // adjoint only: outer points are the forward sources (sp/spf/coef, boxes
+    // obox), inner candidates the forward targets (cell list sstart, tp/tpf,
+    // tbox) with weights wcoef = (w_slp, w_dlp) per target; 7 sums per source
+    // go to gout.
+    int64_t nouter;
+    const int *obox;
+    const double *wcoef;
+    double *gout;
+};
+
+struct GatherAdjArgs {
+    const double2 *sp;    // sorted forward sources
+    int64_t ns;
+    const double *coef;   // 5 per source: f1, f2, S11, S12+S21, S22
+    const double *grid;   // 5 adjoint grids
+    int Mx, My, P;
+    double Lhx, Lhy, h, w, a, scale;
+    const double *e1;
+    double *out;          // 7 per source: 5 values, gradient x, y
 };
 
 struct SpreadArgs {
@@ -215,6 +234,18 @@ cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                         int64_t &launches, bool mixed = false);
 int sm_count();
+cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
+                            int64_t &launches);
+cudaError_t launch_sorted_pair(int64_t n, const int *perm, const double2 *a, const double2 *b,
+                               double *out, cudaStream_t st, int64_t &launches);
+cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &launches);
+cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches);
+cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, const double *gk,
+                                const double *w, int64_t nt, double2 *part,
+                                const double2 *praw, const double2 *fd, const double2 *nrm,
+                                double inv_area, int slp, int dlp, double2 *g_pos,
+                                double2 *g_fs, double2 *g_fd, double2 *g_n, cudaStream_t st,
+                                int64_t &launches);
 cudaError_t launch_spread_f32(const SpreadArgsF &a, int nc, int sms, cudaStream_t st,
                               int64_t &launches);
 cudaError_t launch_filter_f32(const FilterArgsF &a, cudaStream_t st, int64_t &launches);

@@ -122,6 +122,24 @@ __global__ void k_src_coef(int64_t n, const int *__restrict__ perm,
     }
 }
 
+// Sorted copy of two per-point 2-vectors (either may be NULL -> zeros):
+// out[4 j .. 4 j + 3] = (a[perm[j]], b[perm[j]]).
+__global__ void k_sorted_pair(int64_t n, const int *__restrict__ perm,
+                              const double2 *__restrict__ a, const double2 *__restrict__ b,
+                              double *__restrict__ out)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i = perm[j];
+    const double2 x = a ? a[i] : make_double2(0.0, 0.0);
+    const double2 y = b ? b[i] : make_double2(0.0, 0.0);
+    double *o = out + 4 * j;
+    o[0] = x.x;
+    o[1] = x.y;
+    o[2] = y.x;
+    o[3] = y.y;
+}
+
 // ===========================================================================
 // Real-space pair sums (PE/src/mex/StokesSLP/mex_stokes_slp_real.cpp:131-333,
 // PE/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:103-187), SLP and DLP fused.
@@ -687,6 +705,322 @@ template __global__ void k_real<false, true, true>(RealArgs);
 template __global__ void k_real<true, true, true>(RealArgs);
 
 // ===========================================================================
+// Real-space adjoint (source-centric).
+//
+// For J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t) the real-space part
+// contributes, per forward source s and every pair (t, s) of the forward's
+// own pair set (same boxes, same exact cutoff arithmetic, same image shift z
+// of the source seen from the target's box):
+//   SLP  dJ/df_s   += A(d) w_t                 (A symmetric: the forward kernel)
+//        dJ/dy_s   += grad_d [w_t^T A(d) f_s],  E1'(x) = -exp(-x)/x
+//   DLP  dJ/dS_s   += d(w_t . v(d; S))/dS       (S = (S11, S12+S21, S22))
+//        dJ/dy_s   -= grad_d [w_t . v(d; S_s)]  (the DLP enters u with a minus)
+// with d = y_s + z - x_t in each kernel's own rounding order.  One warp per
+// forward source walks the 3x3 neighbourhood of forward targets through the
+// same two pair FIFOs as k_real; lanes keep 7 sums per source.
+// ===========================================================================
+constexpr int kAdjVals = 7;   // gf1, gf2, gS11, gS1221, gS22, gy1, gy2
+
+struct AdjWarp {
+    int2 q[2][64];
+    double acc[kRing][kAdjVals + 1];
+    double2 pos[kRing];
+    int box[kRing];
+    long long idx[kRing];
+    long long tend[2][kRing];
+    int nbs[9], nbp[10];
+    double2 nbz[9];
+    float2 nbzf[9];
+};
+
+template <int NV, class Acc>
+__device__ __forceinline__ void seg_flush_n(Acc &accs, int lane, int key, double *v)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ko = __shfl_up_sync(~0u, key, o);
+        double a[NV];
+#pragma unroll
+        for (int i = 0; i < NV; i++) a[i] = __shfl_up_sync(~0u, v[i], o);
+        if (lane >= o && ko == key) {
+#pragma unroll
+            for (int i = 0; i < NV; i++) v[i] += a[i];
+        }
+    }
+    const int kn = __shfl_down_sync(~0u, key, 1);
+    if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
+        double *a = accs[key % kRing];
+#pragma unroll
+        for (int i = 0; i < NV; i++) a[i] += v[i];
+    }
+    __syncwarp();
+}
+
+template <bool SLP, bool DLP>
+__device__ __forceinline__ void adj_pair(const RealArgs &a, const AdjWarp &W, int2 e,
+                                         const double *tab, const double *e1s, double *g)
+{
+    const int t = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
+    const double2 T = a.tp[t];                  // forward target (inner point)
+    const double2 S = W.pos[slot];              // forward source (outer point)
+    // image shift of the source seen from the target's box: unwrapped source
+    // box = target box - offset k
+    const int tbx = a.tbox[t] % a.nx, tby = a.tbox[t] / a.nx;
+    const int ux = tbx - c_nb_dx[k], uy = tby - c_nb_dy[k];
+    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    const double x1 = (S.x - T.x) + zx, x2 = (S.y - T.y) + zy;          // DLP form
+    const double d1 = S.x - (T.x - zx), d2 = S.y - (T.y - zy);          // SLP form
+    const double *wt = a.wcoef + 4 * (int64_t)t;                         // w_slp, w_dlp of t
+    const double *cs = a.coef + (int64_t)a.nc * W.idx[slot];            // outer coefficients
+    if (SLP && (fl & 1)) {
+        const double r2 = fma(d1, d1, d2 * d2);
+        const double x = r2 * a.xi2;
+        const double ex = exp_neg(x, tab);
+        const double ir2 = rcp_nr(r2);
+        const int set = x >= 16.0 ? 0 : (x > 1.0 ? 1 : 2);
+        const double *c = e1s + 22 * set;
+        const double z = set == 2 ? x : ir2 * a.inv_xi2;
+        double pa = c[0], pb = c[1];
+#pragma unroll
+        for (int i = 2; i < 22; i += 2) {
+            pa = fma(z, pa, c[i]);
+            pb = fma(z, pb, c[i + 1]);
+        }
+        const double den = set == 2 ? pb : pb + x;
+        const double qv = pa * rcp_nr(den);
+        const double E = set == 2 ? qv + x - log(x) - 0.66373538970947265625 : ex * (z + qv);
+        const double w1 = wt[0], w2 = wt[1], f1 = cs[0], f2 = cs[1];
+        const double h = 0.5 * E, gg = ex * ir2;
+        const double gq = gg * fma(d1, w2, -d2 * w1);
+        g[0] = fma(h, w1, fma(gq, d2, g[0]));
+        g[1] = fma(h, w2, fma(-gq, d1, g[1]));
+        // grad_d [w^T A(d) f]
+        const double aa = fma(d1, w1, d2 * w2), bb = fma(d1, f1, d2 * f2), cc = fma(w1, f1, w2 * f2);
+        const double ab = aa * bb;
+        const double kap = ex * (-cc * ir2 - 2.0 * a.xi2 * fma(ab, ir2, -cc) - 2.0 * ab * ir2 * ir2);
+        g[5] = fma(kap, d1, fma(gg, fma(bb, w1, aa * f1), g[5]));
+        g[6] = fma(kap, d2, fma(gg, fma(bb, w2, aa * f2), g[6]));
+    }
+    if (DLP && (fl & 2)) {
+        const double r2 = fma(x1, x1, x2 * x2);
+        const double x = r2 * a.xi2;
+        const double ex = exp_neg(x, tab);
+        const double ir2 = rcp_nr(r2);
+        const double w1 = wt[2], w2 = wt[3];
+        const double *Sc = cs + a.doff;
+        const double S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2];
+        const double fb = -4.0 * (1.0 + x) * ir2 * ir2;
+        const double fbp = 4.0 * (2.0 + x) * ir2 * ir2 * ir2;     // d fb / d r2
+        const double pf = a.pf;
+        const double wd = fma(w1, x1, w2 * x2);
+        // d(w.v)/dS
+        const double fw = fb * wd;
+        g[2] = fma(ex, fma(fw * x1, x1, pf * fma(3.0 * w1, x1, w2 * x2)), g[2]);
+        g[3] = fma(ex, fma(fw * x1, x2, pf * fma(w1, x2, w2 * x1)), g[3]);
+        g[4] = fma(ex, fma(fw * x2, x2, pf * fma(w1, x1, 3.0 * w2 * x2)), g[4]);
+        // grad_d [w.v(d; S)], subtracted (the DLP enters u_dlp with a minus)
+        const double B11 = fma(3.0, S11, S22), B22 = fma(3.0, S22, S11);
+        const double Q = fma(x1 * x1, S11, fma(x1 * x2, S1221, x2 * x2 * S22));
+        const double A1 = fma(B11, x1, S1221 * x2), A2 = fma(S1221, x1, B22 * x2);
+        const double wA = fma(w1, A1, w2 * A2);
+        const double Bw1 = fma(B11, w1, S1221 * w2), Bw2 = fma(S1221, w1, B22 * w2);
+        const double Sd1 = fma(2.0 * S11, x1, S1221 * x2), Sd2 = fma(S1221, x1, 2.0 * S22 * x2);
+        const double radial = -2.0 * a.xi2 * fma(fb * Q, wd, pf * wA) + 2.0 * fbp * Q * wd;
+        const double fbQ = fb * Q, fbw = fb * wd;
+        g[5] -= ex * (radial * x1 + fbw * Sd1 + fbQ * w1 + pf * Bw1);
+        g[6] -= ex * (radial * x2 + fbw * Sd2 + fbQ * w2 + pf * Bw2);
+    }
+}
+
+template <bool SLP, bool DLP>
+__global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
+{
+    __shared__ AdjWarp warps[kRealWarps];
+    __shared__ double tab[64];
+    __shared__ double e1s[66];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
+    for (int i = threadIdx.x; i < 66; i += blockDim.x) e1s[i] = (&c_e1[0][0])[i];
+    __syncthreads();
+    AdjWarp &W = warps[wid];
+    const int64_t nw = (int64_t)gridDim.x * kRealWarps;
+    int head = 0, nfl = 0, gseq = 0;
+    int qn[2] = {0, 0}, tag[2] = {-1, -1};
+    long long enq[2] = {0, 0}, proc[2] = {0, 0};
+    double v[2][kAdjVals];
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < kAdjVals; i++) v[j][i] = 0.0;
+
+    auto batch = [&](int j, int cnt) {
+        const int2 e = lane < cnt ? W.q[j][lane] : make_int2(0, -1);
+        __syncwarp();
+        if (lane < qn[j] - cnt) W.q[j][lane] = W.q[j][lane + cnt];
+        qn[j] -= cnt;
+        proc[j] += cnt;
+        int eseq = -1;
+        if (e.y >= 0) eseq = gseq - nfl + (((e.y & 0xff) - head + kRing) % kRing);
+        const bool fl = tag[j] >= 0 && (lane >= cnt || tag[j] != eseq);
+        if (__any_sync(~0u, fl)) {
+            double tmp[kAdjVals];
+#pragma unroll
+            for (int i = 0; i < kAdjVals; i++) tmp[i] = fl ? v[j][i] : 0.0;
+            seg_flush_n<kAdjVals>(W.acc, lane, tag[j], tmp);
+            if (fl) {
+#pragma unroll
+                for (int i = 0; i < kAdjVals; i++) v[j][i] = 0.0;
+                tag[j] = -1;
+            }
+        }
+        if (lane < cnt) {
+            adj_pair<SLP, DLP>(a, W, e, tab, e1s, v[j]);
+            tag[j] = eseq;
+        }
+    };
+    auto retire = [&](bool all) {
+        while (nfl > 0 && (all || (proc[0] >= W.tend[0][head] + 32 &&
+                                   proc[1] >= W.tend[1][head] + 32))) {
+            if (lane < kAdjVals) a.gout[kAdjVals * W.idx[head] + lane] = W.acc[head][lane];
+            head = (head + 1) % kRing;
+            nfl--;
+        }
+        __syncwarp();
+    };
+    auto drain = [&]() {
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            batch(j, qn[j]);
+            const int key = tag[j] >= 0 ? tag[j] : 0x7fffffff;
+            seg_flush_n<kAdjVals>(W.acc, lane, key, v[j]);
+#pragma unroll
+            for (int i = 0; i < kAdjVals; i++) v[j][i] = 0.0;
+            tag[j] = -1;
+        }
+        retire(true);
+    };
+
+    // outer loop over forward sources (sorted), inner candidates are forward targets
+    for (int64_t s = (int64_t)blockIdx.x * kRealWarps + wid; s < a.nouter; s += nw) {
+        if (nfl == kRing) drain();
+        const int slot = (head + nfl) % kRing;
+        nfl++;
+        gseq++;
+        const int sbx = a.obox[s];
+        const double2 Sp = a.sp[s];
+        const float2 Sf = a.spf[s];
+        if (lane < kAdjVals + 1) W.acc[slot][lane] = 0.0;
+        if (lane == 0) {
+            W.pos[slot] = Sp;
+            W.box[slot] = sbx;
+            W.idx[slot] = s;
+        }
+        int cntk = 0;
+        if (lane < 9) {
+            // target box at offset k from the source box
+            const int ux = sbx % a.nx + c_nb_dx[lane], uy = sbx / a.nx + c_nb_dy[lane];
+            const int wx = (ux + a.nx) % a.nx, wy = (uy + a.ny) % a.ny;
+            const int tb = wy * a.nx + wx;
+            const int b0 = a.sstart[tb];           // target cell list
+            cntk = a.sstart[tb + 1] - b0;
+            W.nbs[lane] = b0;
+            // source image shift seen from that target box (box tb, offset -k)
+            const int vx = wx - c_nb_dx[lane], vy = wy - c_nb_dy[lane];
+            const double zx = vx < 0 ? a.zxm : (vx >= a.nx ? a.zxp : 0.0);
+            const double zy = vy < 0 ? a.zym : (vy >= a.ny ? a.zyp : 0.0);
+            W.nbz[lane] = make_double2(zx, zy);
+            W.nbzf[lane] = make_float2((float)zx, (float)zy);
+        }
+        int incl = cntk;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const int vv = __shfl_up_sync(~0u, incl, o);
+            if (lane >= o) incl += vv;
+        }
+        if (lane < 9) W.nbp[lane + 1] = incl;
+        if (lane == 0) W.nbp[0] = 0;
+        __syncwarp();
+        const int total = W.nbp[9];
+        for (int v0 = 0; v0 < total; v0 += 32) {
+            const int vi = v0 + lane;
+            int fl = 0, t = 0, k = 0;
+            bool nearp = false;
+            if (vi < total) {
+                while (vi >= W.nbp[k + 1]) k++;
+                t = W.nbs[k] + (vi - W.nbp[k]);
+                if (k == 0) {
+                    const double2 T = a.tp[t];
+                    const double dx = xsub(T.x, Sp.x), dy = xsub(T.y, Sp.y);
+                    const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
+                    if (r2 == 0.0) {
+                        // SLP self term: d/df of self_c f.w (mex_stokes_slp_real.cpp:161-163)
+                        if (SLP) {
+                            atomicAdd(&W.acc[slot][0], a.self_c * a.wcoef[4 * (int64_t)t]);
+                            atomicAdd(&W.acc[slot][1], a.self_c * a.wcoef[4 * (int64_t)t + 1]);
+                        }
+                    } else {
+                        fl = 3;
+                        nearp = (float)r2 * a.xi2f <= 1.0f;
+                    }
+                } else {
+                    const float2 Tf = a.tpf[t];
+                    const float2 zf = W.nbzf[k];
+                    const float dxf = Sf.x - (Tf.x - zf.x), dyf = Sf.y - (Tf.y - zf.y);
+                    const float r2f = dxf * dxf + dyf * dyf;
+                    const float ex = 0x1p-22f * (fabsf(Sf.x) + fabsf(Tf.x) + fabsf(zf.x));
+                    const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
+                    const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
+                                               ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
+                    nearp = r2f * a.xi2f <= 1.0f;
+                    if (r2f + band < a.cut2f) {
+                        fl = 3;
+                    } else if (!(r2f - band >= a.cut2f)) {
+                        const double2 T = a.tp[t];
+                        const double2 z = W.nbz[k];
+                        if (SLP) {
+                            const double dx = xsub(Sp.x, xsub(T.x, z.x));
+                            const double dy = xsub(Sp.y, xsub(T.y, z.y));
+                            if (xadd(xmul(dx, dx), xmul(dy, dy)) < a.cut2) fl |= 1;
+                        }
+                        if (DLP) {
+                            const double x1 = xadd(xsub(Sp.x, T.x), z.x);
+                            const double x2 = xadd(xsub(Sp.y, T.y), z.y);
+                            if (xadd(xmul(x1, x1), xmul(x2, x2)) < a.cut2) fl |= 2;
+                        }
+                    }
+                }
+            }
+            if (!SLP) fl &= 2;
+            if (!DLP) fl &= 1;
+            const int2 ent = make_int2(t, slot | (k << 8) | (fl << 12));
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const bool mine = fl != 0 && nearp == (j == 1);
+                const unsigned m = __ballot_sync(~0u, mine);
+                if (mine) W.q[j][qn[j] + __popc(m & ((1u << lane) - 1u))] = ent;
+                qn[j] += __popc(m);
+                enq[j] += __popc(m);
+            }
+            __syncwarp();
+            if (qn[0] >= 32) batch(0, 32);
+            if (qn[1] >= 32) batch(1, 32);
+        }
+        if (lane == 0) {
+            W.tend[0][slot] = enq[0];
+            W.tend[1][slot] = enq[1];
+        }
+        __syncwarp();
+        retire(false);
+    }
+    drain();
+}
+
+template __global__ void k_real_adj<true, false>(RealArgs);
+template __global__ void k_real_adj<false, true>(RealArgs);
+template __global__ void k_real_adj<true, true>(RealArgs);
+
+// ===========================================================================
 // Gaussian spread (fast Gaussian gridding; PE/src/mex/StokesSLP/
 // mex_stokes_slp_kspace.cpp:64-130, PE/src/mex/StokesDLP/
 // mex_stokes_dlp_kspace.cpp:79-150).
@@ -777,6 +1111,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread(SpreadArgs a)
 }
 
 template __global__ void k_spread<2>(SpreadArgs);
+template __global__ void k_spread<4>(SpreadArgs);
 template __global__ void k_spread<3>(SpreadArgs);
 template __global__ void k_spread<5>(SpreadArgs);
 
@@ -963,6 +1298,225 @@ template __global__ void k_gather<2, 12>(GatherArgs);
 template __global__ void k_gather<4, 12>(GatherArgs);
 template __global__ void k_gather<2, 0>(GatherArgs);
 template __global__ void k_gather<4, 0>(GatherArgs);
+
+// ===========================================================================
+// k-space adjoint.
+//
+// The SLP operator grid -> filtered grid is a real circulant with an even,
+// symmetric multiplier, so it is its own transpose: the adjoint spreads w at
+// the targets and runs the same filter.  The DLP operator has the odd
+// multiplier m(k) = -i c(k); its transpose has m(-k) = -m(k), and the minus
+// sign with which the DLP enters u cancels that, so the adjoint applies the
+// transposed 3x2 coefficient matrix with the same -i factor.  Spectra: 0,1 =
+// SLP (in and out), 2,3 = DLP in, 2,3,4 = DLP out.
+// ===========================================================================
+__device__ __forceinline__ void dlp_matrix(double k1, double k2, double xi, double eta,
+                                           double m[2][3])
+{
+    const double K2 = k1 * k1 + k2 * k2;
+    const double e = exp(-0.25 * (1 - eta) / (xi * xi) * K2) / K2 / K2;
+    const double et = e * (1 + 0.25 * K2 / xi / xi);
+    m[0][0] = et * (3.0 * k1 * K2 - 2.0 * k1 * k1 * k1);
+    m[0][1] = et * (k2 * K2 - 2.0 * k1 * k1 * k2);
+    m[0][2] = et * (k1 * K2 - 2.0 * k1 * k2 * k2);
+    m[1][0] = et * (k2 * K2 - 2.0 * k2 * k1 * k1);
+    m[1][1] = et * (k1 * K2 - 2.0 * k2 * k1 * k2);
+    m[1][2] = et * (3.0 * k2 * K2 - 2.0 * k2 * k2 * k2);
+}
+
+__global__ void k_filter_adj(FilterArgs a)
+{
+    const int H = a.My / 2 + 1;
+    const int64_t G = (int64_t)a.Mx * H;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G) return;
+    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    double2 *sp = reinterpret_cast<double2 *>(a.spec);
+    const bool zero = (jx == 0 && jy == 0);
+    const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
+    const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
+    const double k1p = (jx == a.Mx / 2) ? k1 : -k1;
+    const double k2p = (jy == a.My / 2) ? k2 : -k2;
+    const double sc = a.scale;
+    if (a.slp_in >= 0) {
+        double2 o1, o2;
+        const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
+        slp_mode(k1, k2, a.xi, a.eta, h1, h2, o1, o2);
+        if (nyq) {
+            double2 p1, p2;
+            slp_mode(k1p, k2p, a.xi, a.eta, h1, h2, p1, p2);
+            o1.x = 0.5 * (o1.x + p1.x); o1.y = 0.5 * (o1.y + p1.y);
+            o2.x = 0.5 * (o2.x + p2.x); o2.y = 0.5 * (o2.y + p2.y);
+        }
+        if (zero) o1 = o2 = make_double2(0.0, 0.0);
+        sp[a.slp_out * G + idx] = make_double2(o1.x * sc, o1.y * sc);
+        sp[(a.slp_out + 1) * G + idx] = make_double2(o2.x * sc, o2.y * sc);
+    }
+    if (a.dlp_in >= 0) {
+        const double2 p1 = sp[a.dlp_in * G + idx], p2 = sp[(a.dlp_in + 1) * G + idx];
+        double m[2][3];
+        dlp_matrix(k1, k2, a.xi, a.eta, m);
+        if (nyq) {
+            double mp[2][3];
+            dlp_matrix(k1p, k2p, a.xi, a.eta, mp);
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) m[i][c] = 0.5 * (m[i][c] - mp[i][c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            // -i (m_0c p1 + m_1c p2), scaled
+            const double re = m[0][c] * p1.x + m[1][c] * p2.x;
+            const double im = m[0][c] * p1.y + m[1][c] * p2.y;
+            sp[(a.dlp_out + c) * G + idx] = zero ? make_double2(0.0, 0.0)
+                                                 : make_double2(im * sc, -re * sc);
+        }
+    }
+}
+
+// Gather at the forward sources of the adjoint grids, with the gradient of
+// the Gaussian weights: for coefficients c_k (f1, f2, S11, S12+S21, S22)
+//   val_k = s sum_n W_n Phi_k(n),  grad = s sum_n grad_y W_n sum_k c_k Phi_k(n)
+// where d/dp of the weight exponent a(p^2 + 2wp) + a h^2 (i-P/2)^2 - 2ahpi is
+// 2a (p + w - h i).  Output: 7 values per sorted source.
+template <int PT>
+__global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.ns) return;
+    const int P = PT > 0 ? PT : a.P;
+    const size_t G = (size_t)a.Mx * a.My;
+    const double2 S = a.sp[s];
+    int mx, my;
+    double px, py;
+    closest_node(S.x, S.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
+    const double ex = exp(a.a * (px * px + py * py + 2.0 * a.w * px));
+    const double e4y = exp(2.0 * a.a * a.w * py);
+    const double e3x = exp(-2.0 * a.a * a.h * px);
+    const double e3y = exp(-2.0 * a.a * a.h * py);
+    constexpr int PM = (PT > 0 ? PT : kMaxP) + 1;
+    double wy[PM], wyd[PM];
+    {
+        double ey = 1.0;
+#pragma unroll
+        for (int j = 0; j < PM; j++) {
+            if (j <= P) {
+                wy[j] = a.e1[j] * ey;
+                wyd[j] = wy[j] * 2.0 * a.a * (py + a.w - a.h * j);
+                ey *= e3y;
+            }
+        }
+    }
+    double c[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) c[k] = a.coef[5 * s + k];
+    double acc[5] = {0, 0, 0, 0, 0}, gx = 0.0, gy = 0.0;
+    const bool rows_inside = my >= 0 && my + P < a.My;
+    double xf = ex * e4y;
+    for (int i = 0; i <= P; i++) {
+        const double *g = a.grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
+        double tc[5] = {0, 0, 0, 0, 0}, u = 0.0;
+#pragma unroll
+        for (int j = 0; j < PM; j++) {
+            if (j <= P) {
+                const int row = rows_inside ? my + j : wrap_index(my + j, a.My);
+                double cp = 0.0;
+#pragma unroll
+                for (int k = 0; k < 5; k++) {
+                    const double v = __ldg(g + k * G + row);
+                    tc[k] = fma(wy[j], v, tc[k]);
+                    cp = fma(c[k], v, cp);
+                }
+                u = fma(wyd[j], cp, u);
+            }
+        }
+        const double wx = xf * a.e1[i];
+        const double wxd = wx * 2.0 * a.a * (px + a.w - a.h * i);
+        xf *= e3x;
+        double ct = 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            acc[k] = fma(wx, tc[k], acc[k]);
+            ct = fma(c[k], tc[k], ct);
+        }
+        gx = fma(wxd, ct, gx);
+        gy = fma(wx, u, gy);
+    }
+    double *o = a.out + 7 * s;
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = acc[k] * a.scale;
+    o[5] = gx * a.scale;
+    o[6] = gy * a.scale;
+}
+
+template __global__ void k_gather_adj<24>(GatherAdjArgs);
+template __global__ void k_gather_adj<0>(GatherAdjArgs);
+
+// sum_t w_dlp(t) (the zero-mode term's weight), partial sums per block.
+__global__ void __launch_bounds__(256) k_wsum_part(int64_t n, const double *__restrict__ w,
+                                                   int stride, int off, double2 *__restrict__ part)
+{
+    __shared__ double2 red[8];
+    double sx = 0.0, sy = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        sx += w[stride * i + off];
+        sy += w[stride * i + off + 1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(~0u, sx, o);
+        sy += __shfl_xor_sync(~0u, sy, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(sx, sy);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = red[0];
+        for (int k = 1; k < 8; k++) {
+            t.x += red[k].x;
+            t.y += red[k].y;
+        }
+        part[blockIdx.x] = t;
+    }
+}
+
+// Combine the real-space (gr, 7 per sorted source, unscaled) and k-space (gk,
+// 7 per sorted source, scaled) adjoint parts with the DLP zero-mode term and
+// the chain rule S = f (x) n; write gradients in the caller's source order.
+__global__ void k_adj_assemble(int64_t n, const int *__restrict__ perm,
+                               const double *__restrict__ gr, const double *__restrict__ gk,
+                               const double2 *__restrict__ part, int nparts,
+                               const double2 *__restrict__ praw, const double2 *__restrict__ fd,
+                               const double2 *__restrict__ nrm, double inv_area, int slp, int dlp,
+                               double2 *__restrict__ g_pos, double2 *__restrict__ g_fs,
+                               double2 *__restrict__ g_fd, double2 *__restrict__ g_n)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i = perm[j];
+    const double *r = gr + 7 * j, *k = gk + 7 * j;
+    const double q = 1.0 / (4.0 * kPi);
+    double gp1 = r[5] * q + k[5], gp2 = r[6] * q + k[6];
+    if (slp && g_fs) g_fs[i] = make_double2(r[0] * q + k[0], r[1] * q + k[1]);
+    if (dlp) {
+        double Wx = 0.0, Wy = 0.0;
+        for (int b = 0; b < nparts; b++) {
+            Wx += part[b].x;
+            Wy += part[b].y;
+        }
+        const double2 x = praw[i], f = fd[i], m = nrm[i];
+        const double zw = (Wx * x.x + Wy * x.y) * inv_area;        // d J / d (f.n)
+        const double gS11 = -r[2] * q + k[2] + zw, gS12 = -r[3] * q + k[3];
+        const double gS22 = -r[4] * q + k[4] + zw;
+        const double fn = f.x * m.x + f.y * m.y;
+        gp1 += fn * Wx * inv_area;
+        gp2 += fn * Wy * inv_area;
+        if (g_fd) g_fd[i] = make_double2(m.x * gS11 + m.y * gS12, m.x * gS12 + m.y * gS22);
+        if (g_n) g_n[i] = make_double2(f.x * gS11 + f.y * gS12, f.x * gS12 + f.y * gS22);
+    }
+    if (g_pos) g_pos[i] = make_double2(gp1, gp2);
+}
 
 // ===========================================================================
 // Small helpers
@@ -1169,6 +1723,7 @@ cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t 
     switch (nc) {
     case 2: k_spread<2><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     case 3: k_spread<3><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
+    case 4: k_spread<4><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     default: k_spread<5><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     }
     launches++;
@@ -1226,6 +1781,67 @@ cudaError_t launch_assemble(int64_t n, int mode, const int *perm, const double2 
     if (n <= 0) return cudaSuccess;
     k_assemble<<<grid_for(n, 256), 256, 0, st>>>(n, mode, perm, ur, uk, zm, u, ur_out, uk_out);
     launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sorted_pair(int64_t n, const int *perm, const double2 *a, const double2 *b,
+                               double *out, cudaStream_t st, int64_t &launches)
+{
+    if (n <= 0) return cudaSuccess;
+    k_sorted_pair<<<grid_for(n, 256), 256, 0, st>>>(n, perm, a, b, out);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
+                            int64_t &launches)
+{
+    if (a.nouter <= 0) return cudaSuccess;
+    const int64_t want = (a.nouter + kRealWarps - 1) / kRealWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const unsigned g = (unsigned)(want < cap ? want : cap);
+    if (slp && dlp) k_real_adj<true, true><<<g, kRealWarps * 32, 0, st>>>(a);
+    else if (slp) k_real_adj<true, false><<<g, kRealWarps * 32, 0, st>>>(a);
+    else k_real_adj<false, true><<<g, kRealWarps * 32, 0, st>>>(a);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &launches)
+{
+    const int64_t n = (int64_t)a.Mx * (a.My / 2 + 1);
+    k_filter_adj<<<grid_for(n, 256), 256, 0, st>>>(a);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches)
+{
+    if (a.ns <= 0) return cudaSuccess;
+    const unsigned g = grid_for(a.ns, 256);
+    if (a.P == 24) k_gather_adj<24><<<g, 256, 0, st>>>(a);
+    else k_gather_adj<0><<<g, 256, 0, st>>>(a);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, const double *gk,
+                                const double *w, int64_t nt, double2 *part,
+                                const double2 *praw, const double2 *fd, const double2 *nrm,
+                                double inv_area, int slp, int dlp, double2 *g_pos,
+                                double2 *g_fs, double2 *g_fd, double2 *g_n, cudaStream_t st,
+                                int64_t &launches)
+{
+    if (dlp) {
+        k_wsum_part<<<kZeroModeParts, 256, 0, st>>>(nt, w, 4, 2, part);
+        launches++;
+    }
+    if (n > 0) {
+        k_adj_assemble<<<grid_for(n, 256), 256, 0, st>>>(n, perm, gr, gk, part, kZeroModeParts,
+                                                         praw, fd, nrm, inv_area, slp, dlp,
+                                                         g_pos, g_fs, g_fd, g_n);
+        launches++;
+    }
     return cudaGetLastError();
 }
 

@@ -196,6 +196,37 @@ def stokes_ewald(psrc, ptar, f_slp, f_dlp, n, prm: EwaldParams, plan=None):
     return o1.result(), o2.result()
 
 
+def stokes_ewald_adjoint(psrc, ptar, f_slp, f_dlp, n, w_slp, w_dlp, prm: EwaldParams,
+                         plan=None):
+    """Gradients of J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t) (u as returned
+    by :func:`stokes_ewald`) with respect to source positions, SLP forces, DLP
+    densities and normals: returns (g_psrc, g_fslp, g_fdlp, g_n).  Pass None
+    for (f_slp, w_slp) or (f_dlp, n, w_dlp) to drop that term; its gradients
+    come back as None."""
+    pl = _plan(plan)
+    s, t = _Arg(psrc, "psrc"), _Arg(ptar, "ptar")
+    fs, fd, nn = _Arg(f_slp, "f_slp"), _Arg(f_dlp, "f_dlp"), _Arg(n, "n")
+    ws, wd = _Arg(w_slp, "w_slp"), _Arg(w_dlp, "w_dlp")
+    slp = fs.ptr is not None and ws.ptr is not None
+    dlp = fd.ptr is not None and nn.ptr is not None and wd.ptr is not None
+    for a, nm in ((fs, "f_slp"), (fd, "f_dlp"), (nn, "n")):
+        if a.ptr is not None:
+            _same_n(s, a, f"psrc and {nm} must be the same size.")
+    for a, nm in ((ws, "w_slp"), (wd, "w_dlp")):
+        if a.ptr is not None:
+            _same_n(t, a, f"ptar and {nm} must be the same size.")
+    _bind_stream(pl, s.torch)
+    outs = [_Out(s.n, s.torch, pl.device) for _ in range(4)]
+    c = prm.as_c()
+    pl.check(pl.lib.se2p_stokes_ewald_adjoint(
+        pl.handle, ctypes.byref(c), s.ptr, s.n, t.ptr, t.n, fs.ptr if slp else None,
+        fd.ptr if dlp else None, nn.ptr if dlp else None, ws.ptr if slp else None,
+        wd.ptr if dlp else None, outs[0].ptr, outs[1].ptr if slp else None,
+        outs[2].ptr if dlp else None, outs[3].ptr if dlp else None))
+    r = [o.result() for o in outs]
+    return r[0], (r[1] if slp else None), (r[2] if dlp else None), (r[3] if dlp else None)
+
+
 # ----------------------------------------------------------------------------
 # The MATLAB drivers
 # ----------------------------------------------------------------------------

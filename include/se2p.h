@@ -150,6 +150,23 @@ int se2p_stokes_ewald(se2p_plan plan, const se2p_params *prm, const double *psrc
                       int64_t nsrc, const double *ptar, int64_t ntar, const double *f_slp,
                       const double *f_dlp, const double *n, double *u_slp, double *u_dlp);
 
+/* ---- adjoint ---------------------------------------------------------------------
+ * Gradients of J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t), where u_slp and
+ * u_dlp are exactly what se2p_stokes_ewald returns for the same arguments,
+ * with respect to the source positions psrc (as given, before wrapping), the
+ * SLP forces f_slp, the DLP densities f_dlp and the normals n.  The SLP term
+ * is present when f_slp and w_slp are given, the DLP term when f_dlp, n and
+ * w_dlp are; any gradient pointer may be NULL.  Real space is differentiated
+ * over exactly the forward's pair set (E1'(x) = -exp(-x)/x), k space by the
+ * transposed spread/filter/gather chain with the Gaussian weights and their
+ * derivatives recomputed, and the DLP k=0 term analytically.  No reference
+ * counterpart (the reference has no derivatives). */
+int se2p_stokes_ewald_adjoint(se2p_plan plan, const se2p_params *prm, const double *psrc,
+                              int64_t nsrc, const double *ptar, int64_t ntar,
+                              const double *f_slp, const double *f_dlp, const double *n,
+                              const double *w_slp, const double *w_dlp, double *g_psrc,
+                              double *g_fslp, double *g_fdlp, double *g_n);
+
 /* ---- allocation-free SLP real space ------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: a MEX function running inside MATLAB, where gpuArray's caching

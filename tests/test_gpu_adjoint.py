@@ -1,0 +1,138 @@
+"""GPU tests of the adjoint (se2p_stokes_ewald_adjoint) and its torch binding.
+
+J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t).  The hand-written adjoint
+gradients with respect to source positions, SLP forces, DLP densities and
+normals are compared with central finite differences (h = 1e-6) of J, computed
+(a) with the GPU forward, at small and at config-5 size, and (b) with the CPU
+oracle (the reference's algorithm) evaluated on perturbed inputs.  Parameters
+keep the real-space truncation jumps small (xi^2 rc^2 well above 20), so a
+pair crossing the cutoff within +-h cannot spoil the differences.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(N, seed):
+    rng = np.random.default_rng(seed)
+    p = rng.random((2, N))
+    q = rng.random((2, N))
+    f = rng.standard_normal((2, N))
+    g = rng.standard_normal((2, N))
+    th = rng.random(N) * 2 * np.pi
+    n = np.vstack([np.cos(th), np.sin(th)])
+    w1 = rng.standard_normal((2, N))
+    w2 = rng.standard_normal((2, N))
+    return p, q, f, g, n, w1, w2
+
+
+def _J(ft, plan, prm, p, q, f, g, n, w1, w2):
+    us, ud = ft.stokes_ewald(p, q, f, g, n, prm, plan=plan)
+    return float(np.sum(w1 * us) + np.sum(w2 * ud))
+
+
+@pytest.fixture(scope="module")
+def ft():
+    import fasttools2d_gb300 as ft
+    return ft
+
+
+def _check_fd(ft, plan, prm, data, ncoord, seed, evalJ):
+    p, q, f, g, n, w1, w2 = data
+    grads = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm, plan=plan)
+    arrays = [p, f, g, n]
+    rng = np.random.default_rng(seed)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(ncoord):
+        a = int(rng.integers(0, 4))
+        c, i = int(rng.integers(0, 2)), int(rng.integers(0, p.shape[1]))
+        plus = [x.copy() for x in arrays]
+        minus = [x.copy() for x in arrays]
+        plus[a][c, i] += h
+        minus[a][c, i] -= h
+        fd = (evalJ(*plus) - evalJ(*minus)) / (2 * h)
+        scale = np.abs(grads[a]).max()
+        err = abs(fd - grads[a][c, i]) / scale
+        worst = max(worst, err)
+    return worst
+
+
+def test_adjoint_vs_finite_differences_small(ft):
+    N = 1500
+    data = _problem(N, 3)
+    p, q, f, g, n, w1, w2 = data
+    prm = ft.EwaldParams.derived(36.0, 6, 6, 96, 96, 24, 1.0, 1.0)
+    plan = ft.Plan(0)
+    ev = lambda P_, F_, G_, N_: _J(ft, plan, prm, P_, q, F_, G_, N_, w1, w2)
+    assert _check_fd(ft, plan, prm, data, 64, 11, ev) < 2e-6
+    plan.close()
+
+
+def test_adjoint_vs_reference_on_perturbed_inputs(ft):
+    """Finite differences of J computed with the oracle (the reference's algorithm)."""
+    from oracle import oracle as O
+    N = 400
+    data = _problem(N, 5)
+    p, q, f, g, n, w1, w2 = data
+    xi, ns, M, P = 30.0, 5, 80, 24
+    prm = ft.EwaldParams.derived(xi, ns, ns, M, M, P, 1.0, 1.0)
+    plan = ft.Plan(0)
+
+    def ev(P_, F_, G_, N_):
+        us = O.slp_ewald(P_, q, F_, xi, ns, ns, M, M, 1.0, 1.0, P)[0]
+        ud = O.dlp_ewald(P_, q, G_, N_, xi, ns, ns, M, M, 1.0, 1.0, P)[0]
+        return float(np.sum(w1 * us) + np.sum(w2 * ud))
+    assert _check_fd(ft, plan, prm, data, 24, 13, ev) < 2e-6
+    plan.close()
+
+
+def test_adjoint_config5_size(ft):
+    """Config 5: N = 262,144, xi = 430, rc = 0.011 (nside 90), M = 1344, P = 24,
+    64 random coordinates, GPU forward for J."""
+    torch = pytest.importorskip("torch")
+    N = 262144
+    data = _problem(N, 20261203 + 5)
+    p, q, f, g, n, w1, w2 = data
+    prm = ft.EwaldParams.derived(430.0, 90, 90, 1344, 1344, 24, 1.0, 1.0)
+    plan = ft.Plan(0)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    Q, W1, W2 = dev(q), dev(w1), dev(w2)
+
+    def ev(P_, F_, G_, N_):
+        us, ud = ft.stokes_ewald(dev(P_), Q, dev(F_), dev(G_), dev(N_), prm, plan=plan)
+        return float((W1 * us).sum() + (W2 * ud).sum())
+    assert _check_fd(ft, plan, prm, data, 64, 17, ev) < 1e-5
+    plan.close()
+
+
+def test_torch_autograd_binding(ft):
+    torch = pytest.importorskip("torch")
+    from fasttools2d_gb300.autograd import stokes_ewald_torch
+    N = 800
+    p, q, f, g, n, w1, w2 = _problem(N, 9)
+    prm = ft.EwaldParams.derived(30.0, 5, 5, 80, 80, 24, 1.0, 1.0)
+    dev = lambda a, rg=False: torch.from_numpy(np.ascontiguousarray(a.T)).cuda().requires_grad_(rg)
+    P_, F_, G_, N_ = dev(p, True), dev(f, True), dev(g, True), dev(n, True)
+    us, ud = stokes_ewald_torch(P_, dev(q), F_, G_, N_, prm)
+    J = (dev(w1) * us).sum() + (dev(w2) * ud).sum()
+    J.backward()
+    ref = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm)
+    for t_, r_ in zip((P_, F_, G_, N_), ref):
+        got = t_.grad.cpu().numpy().T
+        assert np.abs(got - r_).max() <= 1e-12 * max(1.0, np.abs(r_).max())
+
+
+def test_adjoint_single_kinds_match_fused(ft):
+    N = 1000
+    p, q, f, g, n, w1, w2 = _problem(N, 21)
+    prm = ft.EwaldParams.derived(30.0, 5, 5, 80, 80, 24, 1.0, 1.0)
+    both = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm)
+    s_only = ft.stokes_ewald_adjoint(p, q, f, None, None, w1, None, prm)
+    d_only = ft.stokes_ewald_adjoint(p, q, None, g, n, None, w2, prm)
+    scale = np.abs(both[0]).max()
+    assert np.abs(s_only[0] + d_only[0] - both[0]).max() < 1e-12 * scale
+    assert np.abs(s_only[1] - both[1]).max() < 1e-12 * np.abs(both[1]).max()
+    assert np.abs(d_only[2] - both[2]).max() < 1e-12 * np.abs(both[2]).max()
+    assert s_only[2] is None and d_only[1] is None
