@@ -37,6 +37,7 @@ enum Slot {
     S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM, S_COUNTERS,
     S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
     S_IN_W1, S_IN_W2, S_WCOEF, S_GR, S_GK, S_SBOXS, S_ZEROS,   // adjoint
+    S_FTAB,                                     // cached per-mode filter factors
     S_COUNT_SLOTS
 };
 
@@ -70,6 +71,7 @@ struct se2p_plan_st {
     bool overlap = true;             // real space concurrent with the k-space chain
     bool timing = false;
     bool count_pairs = false;
+    double ftab_key[6] = {0, 0, 0, 0, 0, 0};   // (Mx, My, Lx, Ly, xi, eta) of S_FTAB
     // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NUM_STAGES];
     double stage_ms[T_NUM_STAGES] = {0};
@@ -272,6 +274,25 @@ int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
     CKF(cufftSetStream(p, pl->stream));
     pl->ffts[key] = p;
     *h = p;
+    return SE2P_OK;
+}
+
+// Per-mode filter factors depend only on (Mx, My, Lx, Ly, xi, eta); the plan
+// keeps them between calls, like cuFFT keeps its twiddles.
+int filter_table(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
+{
+    const double key[6] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta};
+    const size_t H = (size_t)fa.Mx * (fa.My / 2 + 1);
+    const bool have = pl->buf[S_FTAB].p && pl->buf[S_FTAB].bytes >= H * sizeof(double2) &&
+                      memcmp(key, pl->ftab_key, sizeof key) == 0;
+    double2 *tab = nullptr;
+    CKS(ensure_t(pl, S_FTAB, H, &tab));
+    if (!have) {
+        fa.etab = nullptr;
+        CK(launch_filter_table(fa, tab, st, pl->launches));
+        memcpy(pl->ftab_key, key, sizeof key);
+    }
+    fa.etab = tab;
     return SE2P_OK;
 }
 
@@ -593,8 +614,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.dlp_in = J.dlp ? doff : -1;
         fa.slp_out = 0;
         fa.dlp_out = J.slp ? 2 : 0;
+        fa.etab = nullptr;
         {
             StageTimer tm(pl, T_FILTER);
+            CKS(filter_table(pl, fa, st));
             CK(launch_filter(fa, st, pl->launches));
         }
 
@@ -845,8 +868,10 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     fa.slp_out = 0;
     fa.dlp_in = 2;
     fa.dlp_out = 2;
+    fa.etab = nullptr;
     {
         StageTimer tm(pl, T_FILTER);
+        CKS(filter_table(pl, fa, st));
         CK(launch_filter_adj(fa, st, pl->launches));
     }
     CKS(get_fft(pl, Mx, My, 5, 1, &inv));

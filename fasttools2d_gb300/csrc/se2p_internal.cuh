@@ -183,6 +183,7 @@ struct FilterArgs {
     double Lx, Ly, xi, eta, scale;   // scale = 1 / (Mx My)
     int slp_in, dlp_in;         // first spectrum of each kind (-1 = absent)
     int slp_out, dlp_out;       // where the 2 filtered spectra of each kind go
+    const double2 *etab;        // per-mode (SLP e, DLP e*t) from k_filter_table, or NULL
 };
 
 struct GatherArgs {
@@ -252,6 +253,8 @@ cudaError_t launch_filter_f32(const FilterArgsF &a, cudaStream_t st, int64_t &la
 cudaError_t launch_gather_f32(const GatherArgsF &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
+cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
+                                int64_t &launches);
 cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_wrap(int64_t n, const double2 *p, double Lx, double Ly, double2 *out,
                         cudaStream_t st, int64_t &launches);

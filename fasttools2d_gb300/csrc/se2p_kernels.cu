@@ -382,12 +382,14 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
     if (DLP && (fl & 2)) {
         const double *Sc = a.coef + (int64_t)a.nc * s + a.doff;
         const double S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2];
-        const double r2d = fma(x1, x1, x2 * x2);
         double xd = x, exd = ex, ird = ir2;
-        if (r2d != r2) {
-            xd = r2d * a.xi2;
-            exd = exp_neg(xd, tab);
-            ird = rcp_nr(r2d);
+        if (zx != 0.0 || zy != 0.0) {          // offsets can differ only across an image
+            const double r2d = fma(x1, x1, x2 * x2);
+            if (r2d != r2) {
+                xd = r2d * a.xi2;
+                exd = exp_neg(xd, tab);
+                ird = rcp_nr(r2d);
+            }
         }
         const double fb = -4.0 * (1.0 + xd) * ird * ird;
         const double Q = fma(x1 * x1, S11, fma(x1 * x2, S1221, x2 * x2 * S22));
@@ -1135,12 +1137,29 @@ __device__ __forceinline__ double kfreq(int j, int M, double L)
     return 2.0 * kPi / L * (double)(j <= M / 2 ? j : j - M);
 }
 
-// SLP filter (mex_stokes_slp_kspace.cpp:197-208) applied to (h1, h2).
+// Per-mode scalar factors of the two filters; they depend on |k|^2 only.
+// SLP: (1/K^4 + 1/(4 xi^2 K^2)) exp(-(1-eta) K^2/(4 xi^2))  (mex_stokes_slp_kspace.cpp:200)
+// DLP: exp(-(1-eta) K^2/(4 xi^2))/K^4 (1 + K^2/(4 xi^2))   (mex_stokes_dlp_kspace.cpp:232-233)
+__device__ __forceinline__ double slp_factor(double K2, double xi, double eta)
+{
+    return (1.0 / (K2 * K2) + 0.25 / (K2 * xi * xi)) * exp(-0.25 * (1 - eta) / (xi * xi) * K2);
+}
+
+__device__ __forceinline__ double dlp_factor(double K2, double xi, double eta)
+{
+    const double e = exp(-0.25 * (1 - eta) / (xi * xi) * K2) / K2 / K2;
+    const double t = 1 + 0.25 * K2 / xi / xi;
+    return e * t;
+}
+
+// SLP filter (mex_stokes_slp_kspace.cpp:197-208) applied to (h1, h2); e < 0
+// means "compute the factor here".
 __device__ __forceinline__ void slp_mode(double k1, double k2, double xi, double eta,
-                                         double2 h1, double2 h2, double2 &o1, double2 &o2)
+                                         double2 h1, double2 h2, double2 &o1, double2 &o2,
+                                         double e = -1.0)
 {
     const double K2 = k1 * k1 + k2 * k2;
-    const double e = (1.0 / (K2 * K2) + 0.25 / (K2 * xi * xi)) * exp(-0.25 * (1 - eta) / (xi * xi) * K2);
+    if (e < 0.0) e = slp_factor(K2, xi, eta);
     o1.x = k2 * (k2 * h1.x - k1 * h2.x) * e;
     o1.y = k2 * (k2 * h1.y - k1 * h2.y) * e;
     o2.x = k1 * (k1 * h2.x - k2 * h1.x) * e;
@@ -1150,18 +1169,16 @@ __device__ __forceinline__ void slp_mode(double k1, double k2, double xi, double
 // DLP filter (mex_stokes_dlp_kspace.cpp:228-251) applied to (h1, h2+h3, h4).
 __device__ __forceinline__ void dlp_mode(double k1, double k2, double xi, double eta,
                                          double2 h1, double2 h23, double2 h4, double2 &o1,
-                                         double2 &o2)
+                                         double2 &o2, double et = -1.0)
 {
     const double K2 = k1 * k1 + k2 * k2;
-    const double e = exp(-0.25 * (1 - eta) / (xi * xi) * K2) / K2 / K2;
-    const double t = 1 + 0.25 * K2 / xi / xi;
+    if (et < 0.0) et = dlp_factor(K2, xi, eta);
     const double B111 = 3.0 * k1 * K2 - 2.0 * k1 * k1 * k1;
     const double B112 = k2 * K2 - 2.0 * k1 * k1 * k2;
     const double B122 = k1 * K2 - 2.0 * k1 * k2 * k2;
     const double B211 = k2 * K2 - 2.0 * k2 * k1 * k1;
     const double B212 = k1 * K2 - 2.0 * k2 * k1 * k2;
     const double B222 = 3.0 * k2 * K2 - 2.0 * k2 * k2 * k2;
-    const double et = e * t;
     o1.x = et * (B111 * h1.x + B112 * h23.x + B122 * h4.x);
     o1.y = et * (B111 * h1.y + B112 * h23.y + B122 * h4.y);
     o2.x = et * (B211 * h1.x + B212 * h23.x + B222 * h4.x);
@@ -1184,12 +1201,15 @@ __global__ void k_filter(FilterArgs a)
     const double k2p = (jy == a.My / 2) ? k2 : -k2;
     const double sc = a.scale;
     double2 so1, so2, do1, do2;
+    // the factors depend on K^2, which k and its partner share; a zero or
+    // non-finite factor (the zero mode) is recomputed inline and discarded
+    const double2 ft = a.etab ? a.etab[idx] : make_double2(-1.0, -1.0);
     if (a.slp_in >= 0) {
         const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
-        slp_mode(k1, k2, a.xi, a.eta, h1, h2, so1, so2);
+        slp_mode(k1, k2, a.xi, a.eta, h1, h2, so1, so2, ft.x);
         if (nyq) {
             double2 p1, p2;
-            slp_mode(k1p, k2p, a.xi, a.eta, h1, h2, p1, p2);
+            slp_mode(k1p, k2p, a.xi, a.eta, h1, h2, p1, p2, ft.x);
             so1.x = 0.5 * (so1.x + p1.x); so1.y = 0.5 * (so1.y + p1.y);
             so2.x = 0.5 * (so2.x + p2.x); so2.y = 0.5 * (so2.y + p2.y);
         }
@@ -1199,10 +1219,10 @@ __global__ void k_filter(FilterArgs a)
     if (a.dlp_in >= 0) {
         const double2 h1 = sp[a.dlp_in * G + idx], h23 = sp[(a.dlp_in + 1) * G + idx];
         const double2 h4 = sp[(a.dlp_in + 2) * G + idx];
-        dlp_mode(k1, k2, a.xi, a.eta, h1, h23, h4, do1, do2);
+        dlp_mode(k1, k2, a.xi, a.eta, h1, h23, h4, do1, do2, ft.y);
         if (nyq) {
             double2 p1, p2;
-            dlp_mode(k1p, k2p, a.xi, a.eta, h1, h23, h4, p1, p2);
+            dlp_mode(k1p, k2p, a.xi, a.eta, h1, h23, h4, p1, p2, ft.y);
             do1.x = 0.5 * (do1.x - p1.x); do1.y = 0.5 * (do1.y - p1.y);
             do2.x = 0.5 * (do2.x - p2.x); do2.y = 0.5 * (do2.y - p2.y);
         }
@@ -1219,6 +1239,24 @@ __global__ void k_filter(FilterArgs a)
         sp[a.dlp_out * G + idx] = do1;
         sp[(a.dlp_out + 1) * G + idx] = do2;
     }
+}
+
+// Per-mode (SLP factor, DLP factor) for the cached filter table; the zero
+// mode, where the factors are not finite, stores -1 (compute inline).
+__global__ void k_filter_table(FilterArgs a, double2 *tab)
+{
+    const int H = a.My / 2 + 1;
+    const int64_t G = (int64_t)a.Mx * H;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G) return;
+    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
+    const double K2 = k1 * k1 + k2 * k2;
+    if (jx == 0 && jy == 0) {
+        tab[idx] = make_double2(-1.0, -1.0);
+        return;
+    }
+    tab[idx] = make_double2(slp_factor(K2, a.xi, a.eta), dlp_factor(K2, a.xi, a.eta));
 }
 
 // ===========================================================================
@@ -1341,10 +1379,11 @@ __global__ void k_filter_adj(FilterArgs a)
     if (a.slp_in >= 0) {
         double2 o1, o2;
         const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
-        slp_mode(k1, k2, a.xi, a.eta, h1, h2, o1, o2);
+        const double fe = a.etab ? a.etab[idx].x : -1.0;
+        slp_mode(k1, k2, a.xi, a.eta, h1, h2, o1, o2, fe);
         if (nyq) {
             double2 p1, p2;
-            slp_mode(k1p, k2p, a.xi, a.eta, h1, h2, p1, p2);
+            slp_mode(k1p, k2p, a.xi, a.eta, h1, h2, p1, p2, fe);
             o1.x = 0.5 * (o1.x + p1.x); o1.y = 0.5 * (o1.y + p1.y);
             o2.x = 0.5 * (o2.x + p2.x); o2.y = 0.5 * (o2.y + p2.y);
         }
@@ -1726,6 +1765,15 @@ cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t 
     case 4: k_spread<4><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     default: k_spread<5><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     }
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
+                                int64_t &launches)
+{
+    const int64_t n = (int64_t)a.Mx * (a.My / 2 + 1);
+    k_filter_table<<<grid_for(n, 256), 256, 0, st>>>(a, tab);
     launches++;
     return cudaGetLastError();
 }
