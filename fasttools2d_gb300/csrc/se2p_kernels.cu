@@ -270,7 +270,7 @@ __constant__ double c_e1[3][22] = {
 // arithmetic", ACM TOMS 15(2), 1989): x = (n/64) ln 2 + r, |r| <= ln2/128,
 // exp(-x) = 2^-(n>>6) * 2^-((n&63)/64) * exp(-r) with a degree-5 Taylor
 // polynomial (truncation < 4e-17).  ln2/64 is split Cody-Waite style (36-bit
-// head).  Returns 0 beyond x = 700 and propagates NaN.
+// head).  Returns 0 from x = 704 on and propagates NaN.
 __device__ __forceinline__ double exp_neg(double x, const double *tab)
 {
     const double kShift = 6755399441055744.0;   // 1.5 * 2^52
@@ -284,9 +284,9 @@ __device__ __forceinline__ double exp_neg(double x, const double *tab)
     p = fma(-r, p, 0.5);
     p = fma(-r, p, 1.0);
     p = fma(-r, p, 1.0);
+    if (__double2hiint(x) >= 0x40860000) return x == x ? 0.0 : x;   // x >= 704, inf, NaN
     const double scale = __hiloint2double((1023 - (n >> 6)) << 20, 0);
-    const double v = p * tab[n & 63] * scale;
-    return x <= 700.0 ? v : (x == x ? 0.0 : x);
+    return p * tab[n & 63] * scale;
 }
 
 // 1/a by the hardware approximation plus two Newton-Raphson steps
@@ -347,12 +347,19 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
     // image shift of neighbour k: 0 or the reference's (L*(+-nside))/nside
     const int tb = W.tbox[slot];
     const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
-    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
-    const double x1 = (S.x - T.x) + zx, x2 = (S.y - T.y) + zy;          // DLP form
-    const double dxs = S.x - (T.x - zx), dys = S.y - (T.y - zy);        // SLP form
-    // The two forms round identically except, rarely, across a periodic
-    // image (z != 0); each kernel then keeps its own r2 as the reference does.
+    // Without a periodic image both offset forms are exactly s - t; across an
+    // image (rare) the SLP form s-(t-z) and the DLP form (s-t)+z are formed
+    // separately and each kernel keeps its own r2, as the reference does.
+    const bool img = ux < 0 || ux >= a.nx || uy < 0 || uy >= a.ny;
+    double x1 = S.x - T.x, x2 = S.y - T.y, dxs = x1, dys = x2;
+    if (img) {
+        const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+        const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+        x1 += zx;
+        x2 += zy;
+        dxs = S.x - (T.x - zx);
+        dys = S.y - (T.y - zy);
+    }
     const double r2 = fma(dxs, dxs, dys * dys);
     const double x = r2 * a.xi2;
     const double ex = exp_neg(x, tab);
@@ -383,7 +390,7 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
         const double *Sc = a.coef + (int64_t)a.nc * s + a.doff;
         const double S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2];
         double xd = x, exd = ex, ird = ir2;
-        if (zx != 0.0 || zy != 0.0) {          // offsets can differ only across an image
+        if (img) {                             // offsets can differ only across an image
             const double r2d = fma(x1, x1, x2 * x2);
             if (r2d != r2) {
                 xd = r2d * a.xi2;

@@ -34,6 +34,7 @@ void mxFree(void *p);
 void mexErrMsgTxt(const char *msg);
 int mexPrintf(const char *fmt, ...);
 int mexCallMATLAB(int nlhs, mxArray *plhs[], int nrhs, mxArray *prhs[], const char *name);
+int mexAtExit(void (*fn)(void));
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);
 #ifdef __cplusplus
 }

@@ -17,6 +17,11 @@ typedef int (*shim_fft_cb)(int inverse, size_t m, size_t n, const double *re,
                            const double *im, double *out_re, double *out_im);
 static shim_fft_cb g_fft = nullptr;
 
+// Functions registered with mexAtExit; shim_run_atexit plays MATLAB's
+// "clear mex" and runs them once.
+static void (*g_atexit[16])(void);
+static int g_natexit = 0;
+
 namespace {
 struct MexError : std::runtime_error {
     explicit MexError(const char *m) : std::runtime_error(m) {}
@@ -75,8 +80,22 @@ int mexCallMATLAB(int nlhs, mxArray *plhs[], int nrhs, mxArray *prhs[], const ch
     return 0;
 }
 
+int mexAtExit(void (*fn)(void))
+{
+    for (int i = 0; i < g_natexit; ++i)
+        if (g_atexit[i] == fn) return 0;
+    if (g_natexit == 16) return 1;
+    g_atexit[g_natexit++] = fn;
+    return 0;
+}
+
 // ---- loader-facing helpers ----------------------------------------------
 void shim_set_fft(shim_fft_cb cb) { g_fft = cb; }
+
+void shim_run_atexit(void)
+{
+    while (g_natexit > 0) g_atexit[--g_natexit]();
+}
 
 typedef void (*mexfn_t)(int, mxArray **, int, const mxArray **);
 

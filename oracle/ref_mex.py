@@ -50,13 +50,16 @@ def _fft2_callback(inverse, m, n, re, im, out_re, out_im):
         return 1
 
 
-class RefMex:
-    """The four reference MEX gateways, callable with MATLAB-shaped numpy args."""
+class MexSet:
+    """Four MEX gateways loaded from ``lib_dir``, called with MATLAB-shaped numpy args.
 
-    def __init__(self):
-        if not available():
-            raise RuntimeError("oracle/_ref not built (run `make -C oracle ref` on x86-64)")
-        self.shim = ctypes.CDLL(os.path.join(REF_DIR, "libmexshim.so"), mode=ctypes.RTLD_GLOBAL)
+    ``shim`` is the MATLAB stand-in they were linked against.  Used for the
+    reference's own gateways (``RefMex``) and for the GPU gateways in
+    ``fasttools2d_gb300/mexgw`` built against the same stand-in.
+    """
+
+    def __init__(self, lib_dir, shim, ext=".so"):
+        self.shim = ctypes.CDLL(shim, mode=ctypes.RTLD_GLOBAL)
         s = self.shim
         s.mxCreateDoubleMatrix.restype = ctypes.c_void_p
         s.mxCreateDoubleMatrix.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int]
@@ -76,9 +79,13 @@ class RefMex:
         s.shim_set_fft(self._cb)
         self.fn = {}
         for n in NAMES:
-            lib = ctypes.CDLL(os.path.join(REF_DIR, n + ".so"), mode=ctypes.RTLD_LOCAL)
+            lib = ctypes.CDLL(os.path.join(lib_dir, n + ext), mode=ctypes.RTLD_LOCAL)
             self.fn[n] = ctypes.cast(lib.mexFunction, ctypes.c_void_p).value
             setattr(self, "_lib_" + n, lib)
+
+    def clear(self):
+        """MATLAB's ``clear mex``: run the functions the gateways gave mexAtExit."""
+        self.shim.shim_run_atexit()
 
     def _mx(self, a):
         a = np.asarray(a, dtype=np.float64)
@@ -123,3 +130,12 @@ class RefMex:
 
     def dlp_kspace(self, psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P):
         return self.call("mex_stokes_dlp_kspace", psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P)
+
+
+class RefMex(MexSet):
+    """The reference's own four MEX gateways compiled under ``oracle/_ref``."""
+
+    def __init__(self):
+        if not available():
+            raise RuntimeError("oracle/_ref not built (run `make -C oracle ref` on x86-64)")
+        super().__init__(REF_DIR, os.path.join(REF_DIR, "libmexshim.so"))
