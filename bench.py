@@ -471,8 +471,10 @@ def gpu_arm(args, rank, world, local_rank):
     plan.set_overlap(True)
 
     # ---- FP32-grid form (config 4) next to the FP64 form on the same workload
-    mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev)
-    adjoint = adjoint_leg(plan, args.steps, timed, dev)
+    legs = set(args.legs.split(","))
+    mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev) \
+        if "fp32_grid" in legs else None
+    adjoint = adjoint_leg(plan, args.steps, timed, dev) if "adjoint" in legs else None
 
     # ---- roofline of the dominant kernel ---------------------------------
     kstages = {k: v for k, v in stages.items() if k not in ("h2d", "d2h") and v[1] > 0}
@@ -519,6 +521,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="points (sources = targets count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--legs", default="fp32_grid,adjoint",
+                    help="extra legs after the headline workload: fp32_grid, adjoint, or none "
+                         "(a profiling run of the headline workload alone uses none)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))

@@ -28,7 +28,9 @@ EXPORTS = (
     "se2p_plan_count_pairs", "se2p_slp_real_noalloc", "se2p_plan_set_precision",
     "se2p_plan_set_overlap", "se2p_stokes_ewald_adjoint",
 )
-PRECISION_FP64, PRECISION_FP32_GRID = 0, 1
+PRECISION_FP64, PRECISION_FP32_GRID, PRECISION_FP64_NATIVE = 0, 1, 2
+_PRECISIONS = {"fp64": PRECISION_FP64, "fp32_grid": PRECISION_FP32_GRID,
+               "fp64_native": PRECISION_FP64_NATIVE}
 
 
 class Se2pError(RuntimeError):
@@ -108,6 +110,7 @@ class Plan:
         if rc != SE2P_OK:
             raise Se2pError(rc, f"cannot create a plan on CUDA device {device}")
         self.device = device
+        self.precision = "fp64"
 
     def check(self, rc):
         if rc != SE2P_OK:
@@ -125,10 +128,11 @@ class Plan:
         return self.lib.se2p_plan_kernel_launches(self.handle)
 
     def set_precision(self, precision):
-        """'fp64' (default) or 'fp32_grid' (mixed precision, tolerances >= 1e-6)."""
-        code = {"fp64": PRECISION_FP64, "fp32_grid": PRECISION_FP32_GRID}.get(precision, precision)
+        """'fp64' (default: FP64 results, float-float hot loops), 'fp64_native'
+        (every operation in FP64) or 'fp32_grid' (mixed precision, tolerances >= 1e-6)."""
+        code = _PRECISIONS.get(precision, precision)
         self.check(self.lib.se2p_plan_set_precision(self.handle, int(code)))
-        self.precision = "fp32_grid" if code == PRECISION_FP32_GRID else "fp64"
+        self.precision = {v: k for k, v in _PRECISIONS.items()}[int(code)]
 
     def set_overlap(self, on: bool = True):
         self.check(self.lib.se2p_plan_set_overlap(self.handle, 1 if on else 0))

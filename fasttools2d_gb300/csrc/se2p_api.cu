@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -38,6 +39,7 @@ enum Slot {
     S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
     S_IN_W1, S_IN_W2, S_WCOEF, S_GR, S_GK, S_SBOXS, S_ZEROS,   // adjoint
     S_FTAB,                                     // cached per-mode filter factors
+    S_GTAB, S_COEF_FF,                          // float-float real space
     S_COUNT_SLOTS
 };
 
@@ -72,6 +74,7 @@ struct se2p_plan_st {
     bool timing = false;
     bool count_pairs = false;
     double ftab_key[6] = {0, 0, 0, 0, 0, 0};   // (Mx, My, Lx, Ly, xi, eta) of S_FTAB
+    bool gtab_ready = false;                   // S_GTAB holds the E1 fit
     // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NUM_STAGES];
     double stage_ms[T_NUM_STAGES] = {0};
@@ -297,6 +300,118 @@ int filter_table(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
 }
 
 // --------------------------------------------------------------------------
+// Piecewise fit of g(x) = exp(x) E1(x) in the reference's Pade form
+// (PE/src/mex/StokesSLP/mex_stokes_slp_real.cpp:19-47: z + p(z)/(q(z) + x),
+// z = 1/x, mid set for 1 < x < 16, far set from 16) for the float-float real
+// space.  Each of the 64 pieces per octave on [1, 64) is interpolated at 7
+// Chebyshev nodes in long double and stored as a degree-6 polynomial in
+// d = x - centre: c0..c3 as float-float, c4..c6 as floats (|c_k d^k| falls
+// by ~2^-7 per degree, so FP32 suffices from c4 on).  Built once per process
+// and checked against the Pade form at 33 points per piece.
+// --------------------------------------------------------------------------
+static const double kE1Host[3][22] = SE2P_E1_PADE;
+
+static long double pade_g(long double x)
+{
+    const double *c = x >= 16 ? kE1Host[0] : kE1Host[1];
+    const long double z = 1.0L / x;
+    long double pa = c[0], pb = c[1];
+    for (int i = 2; i < 22; i += 2) {
+        pa = z * pa + c[i];
+        pb = z * pb + c[i + 1];
+    }
+    return z + pa / (pb + x);
+}
+
+struct GFit {
+    std::vector<float> tab;   // kGPieces x 12 floats
+    double worst = 0;         // largest relative deviation of the stored fit
+};
+
+static const GFit &gfit()
+{
+    static GFit F;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        constexpr int n = 7;
+        const long double pi = 3.141592653589793238462643383279502884L;
+        F.tab.assign((size_t)kGPieces * 12, 0.f);
+        for (int oct = 0; oct < kGOctaves; ++oct)
+            for (int m = 0; m < kGPiecesPerOctave; ++m) {
+                const long double lo = ldexpl(1.0L + m / 64.0L, oct);
+                const long double hi = ldexpl(1.0L + (m + 1) / 64.0L, oct);
+                const long double c = (lo + hi) / 2, hw = (hi - lo) / 2;
+                long double A[n][n + 1];
+                for (int i = 0; i < n; ++i) {
+                    const long double u = cosl(pi * (i + 0.5L) / n);
+                    long double pw = 1;
+                    for (int k = 0; k < n; ++k) {
+                        A[i][k] = pw;
+                        pw *= u;
+                    }
+                    A[i][n] = pade_g(c + hw * u);
+                }
+                for (int col = 0; col < n; ++col) {           // elimination, partial pivoting
+                    int piv = col;
+                    for (int r = col + 1; r < n; ++r)
+                        if (fabsl(A[r][col]) > fabsl(A[piv][col])) piv = r;
+                    for (int k = 0; k <= n; ++k) std::swap(A[col][k], A[piv][k]);
+                    for (int r = 0; r < n; ++r) {
+                        if (r == col) continue;
+                        const long double f = A[r][col] / A[col][col];
+                        for (int k = col; k <= n; ++k) A[r][k] -= f * A[col][k];
+                    }
+                }
+                long double ck[n];
+                long double sc = 1;
+                for (int k = 0; k < n; ++k) {
+                    ck[k] = A[k][n] / A[k][k] / sc;           // coefficient of d^k
+                    sc *= hw;
+                }
+                float *o = F.tab.data() + (size_t)12 * (oct * kGPiecesPerOctave + m);
+                long double stored[n];
+                for (int k = 0; k < 4; ++k) {
+                    const float h = (float)ck[k];
+                    const float l = (float)(ck[k] - h);
+                    o[2 * k] = h;
+                    o[2 * k + 1] = l;
+                    stored[k] = (long double)h + l;
+                }
+                for (int k = 4; k < n; ++k) {
+                    o[4 + k] = (float)ck[k];
+                    stored[k] = o[4 + k];
+                }
+                for (int i = 0; i <= 32; ++i) {
+                    const long double x = lo + (hi - lo) * i / 32.0L * (i == 32 ? 0.999999L : 1);
+                    const long double d = x - c;
+                    long double v = stored[n - 1];
+                    for (int k = n - 2; k >= 0; --k) v = v * d + stored[k];
+                    const long double g = pade_g(x);
+                    F.worst = std::max(F.worst, (double)fabsl((v - g) / g));
+                }
+            }
+    });
+    return F;
+}
+
+// Uploads the fit once per plan; fails if it is not accurate to 1e-14.
+int gtab_device(se2p_plan pl, cudaStream_t st, const float4 **out)
+{
+    const GFit &F = gfit();
+    if (!(F.worst < 1e-14))
+        return fail(pl, SE2P_ERR_UNSUPPORTED, "E1 fit deviates by %.3g", F.worst);
+    float4 *d = nullptr;
+    CKS(ensure_t(pl, S_GTAB, (size_t)kGPieces * 3, &d));
+    if (!pl->gtab_ready) {
+        CK(cudaMemcpyAsync(d, F.tab.data(), F.tab.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));   // the host vector is static, but keep the copy ordered
+        pl->gtab_ready = true;
+    }
+    *out = d;
+    return SE2P_OK;
+}
+
+// --------------------------------------------------------------------------
 // Argument checks (the MEX gateways' checks plus this library's limits)
 // --------------------------------------------------------------------------
 bool finite_pos(double v) { return std::isfinite(v) && v > 0; }
@@ -490,6 +605,24 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             }
             ra.counters = static_cast<unsigned long long *>(pl->buf[S_COUNTERS].p);
         }
+        const int form = pl->precision == SE2P_PRECISION_FP32_GRID    ? kFormF32
+                         : pl->precision == SE2P_PRECISION_FP64_NATIVE ? kFormFP64
+                                                                        : kFormFF;
+        ra.coef_ff = nullptr;
+        ra.ncf = 0;
+        ra.doff_ff = 0;
+        ra.gtab = nullptr;
+        if (form == kFormFF) {
+            const int ncf = (J.slp ? 2 : 0) + (J.dlp ? 5 : 0);
+            float2 *cff = nullptr;
+            CKS(ensure_t(pl, S_COEF_FF, (size_t)ncf * nsz, &cff));
+            CKS(gtab_device(pl, st, &ra.gtab));
+            StageTimer tm(pl, T_COEF);
+            CK(launch_src_coef_ff(ns, coef, nc, J.slp, J.dlp, cff, ncf, st, pl->launches));
+            ra.coef_ff = cff;
+            ra.ncf = ncf;
+            ra.doff_ff = J.slp ? 2 : 0;
+        }
         // Real space on the side stream, overlapping the k-space chain.
         const bool side = J.kspace && pl->overlap;
         cudaStream_t rs = side ? pl->side : st;
@@ -499,8 +632,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         }
         {
             StageTimer tm(pl, T_REAL, rs);
-            CK(launch_real(ra, J.slp, J.dlp, rs, pl->launches,
-                           pl->precision == SE2P_PRECISION_FP32_GRID));
+            CK(launch_real(ra, J.slp, J.dlp, rs, pl->launches, form));
         }
         if (side) CK(cudaEventRecord(pl->join, rs));
     }
@@ -1020,7 +1152,8 @@ int se2p_plan_set_overlap(se2p_plan pl, int on)
 int se2p_plan_set_precision(se2p_plan pl, int precision)
 {
     if (!pl) return SE2P_ERR_ARG;
-    if (precision != SE2P_PRECISION_FP64 && precision != SE2P_PRECISION_FP32_GRID)
+    if (precision != SE2P_PRECISION_FP64 && precision != SE2P_PRECISION_FP32_GRID &&
+        precision != SE2P_PRECISION_FP64_NATIVE)
         return fail(pl, SE2P_ERR_ARG, "unknown precision %d", precision);
     pl->precision = precision;
     return SE2P_OK;

@@ -13,6 +13,50 @@ constexpr double kPi = 3.1415926535897932385;
 // Largest stencil handled: P + 1 nodes per axis must fit one warp.
 constexpr int kMaxP = 30;
 
+// Real-space evaluation forms (k_real template argument).
+constexpr int kFormFP64 = 0;   // every pair in FP64
+constexpr int kFormF32 = 1;    // far pairs in FP32 (FP32-grid precision)
+constexpr int kFormFF = 2;     // far pairs in float-float, near pairs in FP64
+
+// Piecewise fit of g(x) = exp(x) E1(x) in the reference's Pade form on
+// 1 <= x < 64: 64 pieces per octave, degree 6 in d = x - centre; per piece
+// c0..c3 as float-float and c4..c6 as floats, 12 floats (3 float4).
+constexpr int kGPiecesPerOctave = 64;
+constexpr int kGOctaves = 6;
+constexpr int kGPieces = kGPiecesPerOctave * kGOctaves;
+
+// E1 Pade sets of the reference (PE/src/mex/StokesSLP/mex_stokes_slp_real.cpp:19-47)
+// as (numerator, denominator) coefficient pairs, 11 pairs each, highest power
+// first: 0 = far (x >= 16, in 1/x), 1 = mid (1 < x < 16, in 1/x), 2 = near
+// (x <= 1, in x); far and near are padded with leading zeros.  One literal
+// list for the device constant table and the host-side fits.
+#define SE2P_E1_PADE \
+    { \
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+     -17.70313744792479226930481672752649, -2.03222164752550948918496942496859, \
+     -9.56230625623594754358691716333851, 24.24775264986217493401454703416675, \
+     -0.99999982131078080094255255971802, 34.82867640350680460414878325536847, \
+     -0.00000000083503088648841284312372, 11.56228921223568129050818242831156}, \
+    {-1185.45720315201027667, -0.776491285282330997549, \
+     -14751.4895786128450662, 1229.20784182403048905, \
+     -54844.4587226402067411, 18455.4124737722049515, \
+     -86273.1567711649528784, 86722.3403467334749201, \
+     -66598.2652345418633509, 180329.498380501819718, \
+     -27182.6254466733970467, 192104.047790227984431, \
+     -6046.8250112711035463, 113057.05869159631492, \
+     -724.581482791462469795, 38129.5594484818471461, \
+     -43.3058660811817946037, 7417.37624454689546708, \
+     -0.999999999999998811143, 809.193214954550328455, \
+     -0.121013190657725568138e-18, 45.3058660811801465927}, \
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+     -0.000111507792921197858394, -0.528611029520217142048e-6, \
+     -0.00399167106081113256961, 0.000131049900798434683324, \
+     -0.0368031736257943745142, 0.00427347600017103698101, \
+     -0.245088216639761496153, 0.056770677104207528384, \
+     0.0320913665303559189999, 0.37091387659397013215, \
+     0.0865197248079397976498, 1.0}}
+
+
 // ---------------------------------------------------------------------------
 // Never-contracted FP64 arithmetic.  Used wherever the reference's own
 // rounding decides a discrete outcome: the box index of a point, the
@@ -146,6 +190,12 @@ struct RealArgs {
     double2 *u_slp;       // raw sums per sorted target (no 1/(4 pi))
     double2 *u_dlp;
     unsigned long long *counters;   // [candidates, SLP pairs, DLP pairs] (may be NULL)
+    // float-float form only: per sorted source ncf coefficient pairs (SLP f1,
+    // f2; DLP S11, S12+S21, S22, 3 S11 + S22, 3 S22 + S11 from doff_ff) and
+    // the piecewise fit of the E1 Pade form (kGPieces x 3 float4)
+    const float2 *coef_ff;
+    int ncf, doff_ff;
+    const float4 *gtab;
     // adjoint only: outer points are the forward sources (sp/spf/coef, boxes
     // obox), inner candidates the forward targets (cell list sstart, tp/tpf,
     // tbox) with weights wcoef = (w_slp, w_dlp) per target; 7 sums per source
@@ -232,8 +282,10 @@ cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *s
 cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
                             const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
                             cudaStream_t st, int64_t &launches);
+cudaError_t launch_src_coef_ff(int64_t n, const double *coef, int nc, bool slp, bool dlp,
+                               float2 *out, int ncf, cudaStream_t st, int64_t &launches);
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                        int64_t &launches, bool mixed = false);
+                        int64_t &launches, int form = kFormFP64);
 int sm_count();
 cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                             int64_t &launches);

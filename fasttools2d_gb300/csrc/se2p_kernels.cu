@@ -9,6 +9,7 @@
 // work, the spread walks a flattened (P+1)^2 stencil, and the gather gives
 // each lane its own target.  Index, compare and shuffle work is nearly free
 // next to the FP64 pipe.
+#include "se2p_ff.cuh"
 #include "se2p_internal.cuh"
 
 namespace se2p {
@@ -119,6 +120,31 @@ __global__ void k_src_coef(int64_t n, const int *__restrict__ perm,
         c[0] = f.x * m.x;
         c[1] = f.x * m.y + f.y * m.x;
         c[2] = f.y * m.y;
+    }
+}
+
+// Float-float copy of the sorted coefficients for the far pairs of the FP64
+// form: SLP f1, f2; DLP S11, S12+S21, S22 and the combinations 3 S11 + S22,
+// 3 S22 + S11 of the stresslet contraction (formed in FP64, then split).
+__global__ void k_src_coef_ff(int64_t n, const double *__restrict__ coef, int nc, int slp,
+                              int dlp, float2 *__restrict__ out, int ncf)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double *c = coef + (int64_t)nc * j;
+    float2 *o = out + (int64_t)ncf * j;
+    if (slp) {
+        o[0] = ff_split(c[0]);
+        o[1] = ff_split(c[1]);
+        c += 2;
+        o += 2;
+    }
+    if (dlp) {
+        o[0] = ff_split(c[0]);
+        o[1] = ff_split(c[1]);
+        o[2] = ff_split(c[2]);
+        o[3] = ff_split(fma(3.0, c[0], c[2]));
+        o[4] = ff_split(fma(3.0, c[2], c[0]));
     }
 }
 
@@ -237,33 +263,8 @@ __constant__ double c_exp_tab[64] = {
     0x1.059b0d3158574p-1,
     0x1.02c9a3e778061p-1};
 
-// E1 Pade sets as (numerator, denominator) pairs, 11 pairs each, highest
-// power first: 0 = far (x >= 16, in 1/x), 1 = mid (1 < x < 16, in 1/x),
-// 2 = near (x <= 1, in x); far and near are padded with leading zeros.
-__constant__ double c_e1[3][22] = {
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-     -17.70313744792479226930481672752649, -2.03222164752550948918496942496859,
-     -9.56230625623594754358691716333851, 24.24775264986217493401454703416675,
-     -0.99999982131078080094255255971802, 34.82867640350680460414878325536847,
-     -0.00000000083503088648841284312372, 11.56228921223568129050818242831156},
-    {-1185.45720315201027667, -0.776491285282330997549,
-     -14751.4895786128450662, 1229.20784182403048905,
-     -54844.4587226402067411, 18455.4124737722049515,
-     -86273.1567711649528784, 86722.3403467334749201,
-     -66598.2652345418633509, 180329.498380501819718,
-     -27182.6254466733970467, 192104.047790227984431,
-     -6046.8250112711035463, 113057.05869159631492,
-     -724.581482791462469795, 38129.5594484818471461,
-     -43.3058660811817946037, 7417.37624454689546708,
-     -0.999999999999998811143, 809.193214954550328455,
-     -0.121013190657725568138e-18, 45.3058660811801465927},
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-     -0.000111507792921197858394, -0.528611029520217142048e-6,
-     -0.00399167106081113256961, 0.000131049900798434683324,
-     -0.0368031736257943745142, 0.00427347600017103698101,
-     -0.245088216639761496153, 0.056770677104207528384,
-     0.0320913665303559189999, 0.37091387659397013215,
-     0.0865197248079397976498, 1.0}};
+// The three E1 Pade sets (layout in se2p_internal.cuh).
+__constant__ double c_e1[3][22] = SE2P_E1_PADE;
 
 // exp(-x) for x >= 0 by Tang's table-driven method (P. T. P. Tang, "Table-
 // driven implementation of the exponential function in IEEE floating-point
@@ -486,6 +487,76 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
     }
 }
 
+// g(x) = exp(x) E1(x) in the reference's Pade form (mid set below 16, far
+// set from 16 on), from the piecewise fit gtab, for 1 < x < 64.  The piece
+// follows from the head's exponent and top six mantissa bits; x = 16 with a
+// negative tail belongs to the mid set's last piece.
+__device__ __forceinline__ float2 ff_g_e1(float2 x, const float4 *__restrict__ gtab)
+{
+    const unsigned xb = __float_as_uint(x.x);
+    int oct = (int)(xb >> 23) - 127;
+    int m = (int)((xb >> 17) & 63u);
+    if (x.x == 16.0f && x.y < 0.0f) {
+        oct = 3;
+        m = 63;
+    }
+    const float c = __uint_as_float(((unsigned)(oct + 127) << 23) | ((unsigned)m << 17) | (1u << 16));
+    float dh, dl;
+    fast_two_sum(x.x - c, x.y, dh, dl);           // x.x - c is exact (same binade)
+    const float2 d = make_float2(dh, dl);
+    const float4 *cf = gtab + 3 * (oct * kGPiecesPerOctave + m);
+    const float4 A = __ldg(cf), B = __ldg(cf + 1), C = __ldg(cf + 2);
+    const float t = fmaf(fmaf(C.z, dh, C.y), dh, C.x);
+    float2 p = ff_add(make_float2(B.z, B.w), ff_mul_f(d, t));
+    p = ff_add(make_float2(B.x, B.y), ff_mul(p, d));
+    p = ff_add(make_float2(A.z, A.w), ff_mul(p, d));
+    return ff_add(make_float2(A.x, A.y), ff_mul(p, d));
+}
+
+// A pair in float-float (FP64 form, far pairs 1 < xi^2 r^2 < 64): the offset
+// is formed in FP64 (s - t, plus the image shift), split, and everything
+// after runs on the FP32 pipe: r^2, x = xi^2 r^2, exp(-x) (Tang), 1/r^2
+// (Newton), E1 = exp(-x) g(x), and the SLP / DLP contractions of real_pair.
+template <bool SLP, bool DLP>
+__device__ __forceinline__ void real_pair_ff(const RealArgs &a, const RealWarp &W, int2 e,
+                                             const float2 *tabff, float2 xi2, float2 pf,
+                                             float2 &s1, float2 &s2, float2 &d1, float2 &d2)
+{
+    const int s = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
+    const double2 S = a.sp[s];
+    const double2 T = W.tpos[slot];
+    // image shift of neighbour k of this pair's target (the FIFO outlives W.nbz)
+    const int tb = W.tbox[slot];
+    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    const float2 x1 = ff_split((S.x - T.x) + zx), x2 = ff_split((S.y - T.y) + zy);
+    const float2 r2 = ff_add(ff_sqr(x1), ff_sqr(x2));
+    const float2 x = ff_mul(r2, xi2);
+    const float2 ex = ff_exp_neg(x, tabff);
+    const float2 ir2 = ff_rcp(r2);
+    const float2 *cf = a.coef_ff + (int64_t)a.ncf * s;
+    if (SLP && (fl & 1)) {
+        const float2 f1 = cf[0], f2 = cf[1];
+        const float2 h = ff_scale(ff_mul(ex, ff_g_e1(x, a.gtab)), 0.5f);
+        const float2 gq = ff_mul(ff_mul(ex, ir2), ff_sub(ff_mul(x1, f2), ff_mul(x2, f1)));
+        s1 = ff_add(s1, ff_add(ff_mul(h, f1), ff_mul(gq, x2)));
+        s2 = ff_add(s2, ff_sub(ff_mul(h, f2), ff_mul(gq, x1)));
+    }
+    if (DLP && (fl & 2)) {
+        const float2 *Sc = cf + a.doff_ff;
+        const float2 S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2], T1 = Sc[3], T2 = Sc[4];
+        const float2 fb = ff_scale(ff_mul(ff_add_f(x, 1.0f), ff_sqr(ir2)), -4.0f);
+        const float2 Q = ff_add(ff_add(ff_mul(ff_sqr(x1), S11), ff_mul(ff_mul(x1, x2), S1221)),
+                                ff_mul(ff_sqr(x2), S22));
+        const float2 A1 = ff_add(ff_mul(x1, T1), ff_mul(x2, S1221));
+        const float2 A2 = ff_add(ff_mul(x2, T2), ff_mul(x1, S1221));
+        const float2 fq = ff_mul(fb, Q);
+        d1 = ff_add(d1, ff_mul(ex, ff_add(ff_mul(fq, x1), ff_mul(pf, A1))));
+        d2 = ff_add(d2, ff_mul(ex, ff_add(ff_mul(fq, x2), ff_mul(pf, A2))));
+    }
+}
+
 // Lane-side state of one pair FIFO.
 struct PairQueue {
     int qn;               // entries queued (warp-uniform)
@@ -493,17 +564,27 @@ struct PairQueue {
     int tag;              // sequence number of the target this lane's sums belong to
     double s1, s2, d1, d2;
     float f1, f2, g1, g2; // FP32 sums of the mixed-precision form
+    float2 h1, h2, k1, k2; // float-float sums of the FP64 form's far pairs
 };
 
-template <bool SLP, bool DLP, bool MIXED>
+template <bool SLP, bool DLP, int FORM>
 __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
 {
+    constexpr bool MIXED = FORM == kFormF32;
+    constexpr bool FF = FORM == kFormFF;
     __shared__ RealWarp warps[kRealWarps];
     __shared__ double tab[64];
+    __shared__ float2 tabff[64];
     __shared__ double e1s[66];
     __shared__ float e1f[66];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+        tab[i] = c_exp_tab[i];
+        tabff[i] = ff_split(c_exp_tab[i]);
+    }
+    const float2 xi2ff = ff_split(a.xi2), pfff = ff_split(a.pf);
+    // float-float pairs: 1 < x < 64 with margins for the FP32 pre-test
+    const float xlo = FF ? 1.0001f : 1.0f, xhi = FF ? 63.9f : INFINITY;
     for (int i = threadIdx.x; i < 66; i += blockDim.x) {
         e1s[i] = (&c_e1[0][0])[i];
         e1f[i] = (&c_e1f[0][0])[i];
@@ -519,6 +600,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         Q[j].qn = 0; Q[j].enq = 0; Q[j].proc = 0; Q[j].tag = -1;
         Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
         Q[j].f1 = Q[j].f2 = Q[j].g1 = Q[j].g2 = 0.f;
+        Q[j].h1 = Q[j].h2 = Q[j].k1 = Q[j].k2 = make_float2(0.f, 0.f);
     }
     unsigned long long ncand = 0, nslp = 0, ndlp = 0;
 
@@ -535,18 +617,28 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         if (e.y >= 0) eseq = gseq - nfl + (((e.y & 0xff) - head + kRing) % kRing);
         const bool fl = P.tag >= 0 && (lane >= cnt || P.tag != eseq);
         const bool f32 = MIXED && j == 0;
+        const bool ffp = FF && j == 0;
         if (__any_sync(~0u, fl)) {
-            const double v0 = f32 ? (double)P.f1 : P.s1, v1 = f32 ? (double)P.f2 : P.s2;
-            const double v2 = f32 ? (double)P.g1 : P.d1, v3 = f32 ? (double)P.g2 : P.d2;
+            double v0 = P.s1, v1 = P.s2, v2 = P.d1, v3 = P.d2;
+            if (f32) {
+                v0 = (double)P.f1; v1 = (double)P.f2; v2 = (double)P.g1; v3 = (double)P.g2;
+            }
+            if (ffp) {
+                v0 = ff_to_double(P.h1); v1 = ff_to_double(P.h2);
+                v2 = ff_to_double(P.k1); v3 = ff_to_double(P.k2);
+            }
             seg_flush(W, lane, P.tag, fl ? v0 : 0.0, fl ? v1 : 0.0, fl ? v2 : 0.0, fl ? v3 : 0.0);
             if (fl) {
                 P.s1 = P.s2 = P.d1 = P.d2 = 0.0;
                 P.f1 = P.f2 = P.g1 = P.g2 = 0.f;
+                P.h1 = P.h2 = P.k1 = P.k2 = make_float2(0.f, 0.f);
                 P.tag = -1;
             }
         }
         if (lane < cnt) {
             if (f32) real_pair_f32<SLP, DLP>(a, W, e, e1f, P.f1, P.f2, P.g1, P.g2);
+            else if (ffp)
+                real_pair_ff<SLP, DLP>(a, W, e, tabff, xi2ff, pfff, P.h1, P.h2, P.k1, P.k2);
             else real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
             P.tag = eseq;
         }
@@ -573,10 +665,14 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
             if (MIXED && j == 0)
                 seg_flush(W, lane, key, (double)Q[j].f1, (double)Q[j].f2, (double)Q[j].g1,
                           (double)Q[j].g2);
+            else if (FF && j == 0)
+                seg_flush(W, lane, key, ff_to_double(Q[j].h1), ff_to_double(Q[j].h2),
+                          ff_to_double(Q[j].k1), ff_to_double(Q[j].k2));
             else
                 seg_flush(W, lane, key, Q[j].s1, Q[j].s2, Q[j].d1, Q[j].d2);
             Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
             Q[j].f1 = Q[j].f2 = Q[j].g1 = Q[j].g2 = 0.f;
+            Q[j].h1 = Q[j].h2 = Q[j].k1 = Q[j].k2 = make_float2(0.f, 0.f);
             Q[j].tag = -1;
         }
         retire(true);
@@ -641,7 +737,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                         }
                     } else {
                         fl = 3;
-                        nearp = (float)r2 * a.xi2f <= 1.0f;
+                        const float xf = (float)r2 * a.xi2f;
+                        nearp = !(xf > xlo && xf < xhi);
                     }
                 } else {
                     const float2 Sf = a.spf[s];
@@ -654,7 +751,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                     const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
                     const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
                                                ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
-                    nearp = r2f * a.xi2f <= 1.0f;
+                    const float xf = r2f * a.xi2f;
+                    nearp = !(xf > xlo && xf < xhi);
                     if (r2f + band < a.cut2f) {
                         fl = 3;
                     } else if (!(r2f - band >= a.cut2f)) {
@@ -706,12 +804,15 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
     }
 }
 
-template __global__ void k_real<true, false, false>(RealArgs);
-template __global__ void k_real<false, true, false>(RealArgs);
-template __global__ void k_real<true, true, false>(RealArgs);
-template __global__ void k_real<true, false, true>(RealArgs);
-template __global__ void k_real<false, true, true>(RealArgs);
-template __global__ void k_real<true, true, true>(RealArgs);
+template __global__ void k_real<true, false, kFormFP64>(RealArgs);
+template __global__ void k_real<false, true, kFormFP64>(RealArgs);
+template __global__ void k_real<true, true, kFormFP64>(RealArgs);
+template __global__ void k_real<true, false, kFormF32>(RealArgs);
+template __global__ void k_real<false, true, kFormF32>(RealArgs);
+template __global__ void k_real<true, true, kFormF32>(RealArgs);
+template __global__ void k_real<true, false, kFormFF>(RealArgs);
+template __global__ void k_real<false, true, kFormFF>(RealArgs);
+template __global__ void k_real<true, true, kFormFF>(RealArgs);
 
 // ===========================================================================
 // Real-space adjoint (source-centric).
@@ -852,6 +953,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
     for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
     for (int i = threadIdx.x; i < 66; i += blockDim.x) e1s[i] = (&c_e1[0][0])[i];
     __syncthreads();
+    const float xlo = 1.0f, xhi = INFINITY;   // near FIFO: x <= 1 (all pairs FP64)
     AdjWarp &W = warps[wid];
     const int64_t nw = (int64_t)gridDim.x * kRealWarps;
     int head = 0, nfl = 0, gseq = 0;
@@ -970,7 +1072,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
                         }
                     } else {
                         fl = 3;
-                        nearp = (float)r2 * a.xi2f <= 1.0f;
+                        const float xf = (float)r2 * a.xi2f;
+                        nearp = !(xf > xlo && xf < xhi);
                     }
                 } else {
                     const float2 Tf = a.tpf[t];
@@ -981,7 +1084,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
                     const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
                     const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
                                                ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
-                    nearp = r2f * a.xi2f <= 1.0f;
+                    const float xf = r2f * a.xi2f;
+                    nearp = !(xf > xlo && xf < xhi);
                     if (r2f + band < a.cut2f) {
                         fl = 3;
                     } else if (!(r2f - band >= a.cut2f)) {
@@ -1739,22 +1843,33 @@ cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
     return cudaGetLastError();
 }
 
+cudaError_t launch_src_coef_ff(int64_t n, const double *coef, int nc, bool slp, bool dlp,
+                               float2 *out, int ncf, cudaStream_t st, int64_t &launches)
+{
+    if (n <= 0) return cudaSuccess;
+    k_src_coef_ff<<<grid_for(n, 256), 256, 0, st>>>(n, coef, nc, slp, dlp, out, ncf);
+    launches++;
+    return cudaGetLastError();
+}
+
+template <int FORM>
+static void launch_real_form(const RealArgs &a, bool slp, bool dlp, unsigned g, cudaStream_t st)
+{
+    if (slp && dlp) k_real<true, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+    else if (slp) k_real<true, false, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+    else k_real<false, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+}
+
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                        int64_t &launches, bool mixed)
+                        int64_t &launches, int form)
 {
     if (a.ntar <= 0) return cudaSuccess;
     const int64_t want = (a.ntar + kRealWarps - 1) / kRealWarps;
     const int64_t cap = (int64_t)sm_count() * 8;
     const unsigned g = (unsigned)(want < cap ? want : cap);
-    if (mixed) {
-        if (slp && dlp) k_real<true, true, true><<<g, kRealWarps * 32, 0, st>>>(a);
-        else if (slp) k_real<true, false, true><<<g, kRealWarps * 32, 0, st>>>(a);
-        else k_real<false, true, true><<<g, kRealWarps * 32, 0, st>>>(a);
-    } else {
-        if (slp && dlp) k_real<true, true, false><<<g, kRealWarps * 32, 0, st>>>(a);
-        else if (slp) k_real<true, false, false><<<g, kRealWarps * 32, 0, st>>>(a);
-        else k_real<false, true, false><<<g, kRealWarps * 32, 0, st>>>(a);
-    }
+    if (form == kFormF32) launch_real_form<kFormF32>(a, slp, dlp, g, st);
+    else if (form == kFormFF) launch_real_form<kFormFF>(a, slp, dlp, g, st);
+    else launch_real_form<kFormFP64>(a, slp, dlp, g, st);
     launches++;
     return cudaGetLastError();
 }

@@ -72,15 +72,28 @@ int64_t se2p_plan_kernel_launches(se2p_plan plan);
 const char *se2p_version(void);
 
 /* ---- precision ----------------------------------------------------------------
- * SE2P_PRECISION_FP64 (default): every step in FP64, matching the reference
- * to <= 1e-12.  SE2P_PRECISION_FP32_GRID: the mixed form for tolerances
- * >= 1e-6 -- spreading, FFT, filter and gather in FP32 and the far real-space
- * pairs (xi^2 r^2 > 1) in FP32, while the near real-space pairs (E1 at small
+ * SE2P_PRECISION_FP64 (default): FP64 inputs, outputs, grids and k-space
+ * arithmetic; results within <= 1e-12 of the reference.  The far real-space
+ * pairs (1 < xi^2 r^2 < 64) are evaluated in float-float arithmetic -- pairs
+ * of FP32 values carrying about 48 bits -- because GB300 issues FP32 some 70
+ * times faster than FP64; the real-space sum is well conditioned, so this
+ * moves results by ~1e-15.  Near pairs, the SLP self term and the k-space
+ * chain (spread, FFT, filter, gather, whose DLP part amplifies rounding
+ * ~1000-fold) stay FP64.
+ * SE2P_PRECISION_FP64_NATIVE: every floating-point step an FP64 instruction,
+ * as the reference computes it.
+ * SE2P_PRECISION_FP32_GRID: the mixed form for tolerances >= 1e-6 --
+ * spreading, FFT, filter and gather in FP32 and the far real-space pairs
+ * (xi^2 r^2 > 1) in FP32, while the near real-space pairs (E1 at small
  * argument), the SLP self term and the DLP k=0 term stay FP64; the pair set,
- * box assignment and stencil origins stay exactly the reference's.  No
- * reference counterpart (the reference is FP64 only).  Applies to all later
- * calls on the plan. */
-typedef enum { SE2P_PRECISION_FP64 = 0, SE2P_PRECISION_FP32_GRID = 1 } se2p_precision;
+ * box assignment and stencil origins stay exactly the reference's.
+ * No reference counterpart (the reference is FP64 only).  Applies to all
+ * later calls on the plan. */
+typedef enum {
+    SE2P_PRECISION_FP64 = 0,
+    SE2P_PRECISION_FP32_GRID = 1,
+    SE2P_PRECISION_FP64_NATIVE = 2
+} se2p_precision;
 int se2p_plan_set_precision(se2p_plan plan, int precision);
 
 /* ---- stage timing ------------------------------------------------------------

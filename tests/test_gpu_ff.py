@@ -1,0 +1,98 @@
+"""The FP64 form's float-float real space against the all-FP64 form.
+
+SE2P_PRECISION_FP64 (the default) evaluates the far real-space pairs
+(1 < xi^2 r^2 < 64) in float-float arithmetic (about 48 significant bits);
+SE2P_PRECISION_FP64_NATIVE issues every operation as an FP64 instruction.
+Both must match the reference's outputs in tests/golden to <= 1e-12
+(normwise relative).  The real-space sum is well conditioned, so the two
+forms agree to ~1e-15; the bound used here is 2e-14.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, relerr
+
+pytestmark = pytest.mark.gpu
+PARITY = 1e-12
+FF_VS_NATIVE = 2e-14
+
+
+@pytest.fixture(scope="module")
+def ft():
+    import fasttools2d_gb300 as ft
+    return ft
+
+
+@pytest.fixture(scope="module")
+def plans(ft):
+    ff, nat = ft.Plan(0), ft.Plan(0)
+    nat.set_precision("fp64_native")
+    assert ff.precision == "fp64" and nat.precision == "fp64_native"
+    yield ff, nat
+    ff.close()
+    nat.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_both_forms_match_reference(ft, plans, name):
+    g = load_golden(name)
+    ps, pt, f, n = g["psrc"], g["ptar"], g["f"], g["n"]
+    for plan in plans:
+        u = ft.mex_stokes_slp_real(ps, pt, f, g["xi"], g["nside_x"], g["nside_y"], g["Lx"],
+                                   g["Ly"], plan=plan)
+        assert relerr(u, g["out_slp_real"]) < PARITY, (plan.precision, "slp")
+        u = ft.mex_stokes_dlp_real(ps, pt, f, n, g["xi"], g["nside_x"], g["nside_y"], g["Lx"],
+                                   g["Ly"], plan=plan)
+        assert relerr(u, g["out_dlp_real"]) < PARITY, (plan.precision, "dlp")
+    args = (g["Mx"], g["My"], g["Lx"], g["Ly"], g["w"], g["P"])
+    u = ft.mex_stokes_dlp_kspace(ps, pt, g["xi"], g["eta"], f, n, *args, plan=plans[1])
+    assert relerr(u, g["out_dlp_kspace"]) < PARITY
+
+
+def _cloud(N, seed):
+    rng = np.random.default_rng(seed)
+    p = rng.random((2, N))
+    q = rng.random((2, N))
+    f = rng.standard_normal((2, N))
+    g = rng.standard_normal((2, N))
+    th = rng.random(N) * 2 * np.pi
+    return p, q, f, g, np.vstack([np.cos(th), np.sin(th)])
+
+
+@pytest.mark.parametrize("xi,nside", [(120.0, 30), (60.0, 12), (300.0, 20), (20.0, 3)])
+def test_ff_real_space_agrees_with_native(ft, plans, xi, nside):
+    """xi^2 rc^2 spans 16 (few far pairs) to 1e4 (many pairs beyond x = 64,
+    which go to the FP64 queue)."""
+    ff, nat = plans
+    p, q, f, g, n = _cloud(20000, int(xi))
+    for fn, args in ((ft.mex_stokes_slp_real, (p, q, f)), (ft.mex_stokes_dlp_real, (p, q, f, n))):
+        a = fn(*args, xi, nside, nside, 1.0, 1.0, plan=ff)
+        b = fn(*args, xi, nside, nside, 1.0, 1.0, plan=nat)
+        assert relerr(a, b) < FF_VS_NATIVE, (fn.__name__, relerr(a, b))
+
+
+def test_ff_clustered_and_coincident(ft, plans):
+    """Clustered sources, exact coincidences (SLP self term, DLP skip) and
+    targets on periodic images of sources (NaN in both forms)."""
+    ff, nat = plans
+    rng = np.random.default_rng(9)
+    c = rng.random((2, 40))
+    p = (c[:, rng.integers(0, 40, 6000)] + 0.004 * rng.standard_normal((2, 6000))) % 1.0
+    q = np.hstack([p[:, :500], rng.random((2, 3000))])
+    f = rng.standard_normal((2, 6000))
+    th = rng.random(6000) * 2 * np.pi
+    n = np.vstack([np.cos(th), np.sin(th)])
+    for fn, args in ((ft.mex_stokes_slp_real, (p, q, f)), (ft.mex_stokes_dlp_real, (p, q, f, n))):
+        a = fn(*args, 150.0, 20, 20, 1.0, 1.0, plan=ff)
+        b = fn(*args, 150.0, 20, 20, 1.0, 1.0, plan=nat)
+        assert relerr(a, b) < FF_VS_NATIVE, (fn.__name__, relerr(a, b))
+
+
+def test_ff_composite_agrees_with_native(ft, plans):
+    ff, nat = plans
+    p, q, f, g, n = _cloud(50000, 7)
+    prm = ft.EwaldParams.derived(200.0, 45, 45, 640, 640, 24, 1.0, 1.0)
+    us, ud = ft.stokes_ewald(p, q, f, g, n, prm, plan=ff)
+    vs, vd = ft.stokes_ewald(p, q, f, g, n, prm, plan=nat)
+    assert relerr(us, vs) < FF_VS_NATIVE and relerr(ud, vd) < FF_VS_NATIVE, \
+        (relerr(us, vs), relerr(ud, vd))
