@@ -942,9 +942,12 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
         CK(cudaEventRecord(pl->fork, st));
         CK(cudaStreamWaitEvent(rs, pl->fork, 0));
     }
+    const int form = pl->precision == SE2P_PRECISION_FP64_NATIVE ? kFormFP64 : kFormFF;
+    ra.gtab = nullptr;
+    if (form == kFormFF) CKS(gtab_device(pl, st, &ra.gtab));
     {
         StageTimer tm(pl, T_REAL, rs);
-        CK(launch_real_adj(ra, slp, dlp, rs, pl->launches));
+        CK(launch_real_adj(ra, slp, dlp, rs, pl->launches, form));
     }
     if (side) CK(cudaEventRecord(pl->join, rs));
 

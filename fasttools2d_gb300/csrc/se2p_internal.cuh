@@ -288,7 +288,7 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                         int64_t &launches, int form = kFormFP64);
 int sm_count();
 cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                            int64_t &launches);
+                            int64_t &launches, int form = kFormFP64);
 cudaError_t launch_sorted_pair(int64_t n, const int *perm, const double2 *a, const double2 *b,
                                double *out, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &launches);

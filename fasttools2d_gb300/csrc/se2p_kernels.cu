@@ -943,23 +943,118 @@ __device__ __forceinline__ void adj_pair(const RealArgs &a, const AdjWarp &W, in
     }
 }
 
+// adj_pair in float-float for the far pairs (1 < xi^2 r^2 < 64) of the FP64
+// form: same terms, same pair, evaluated as in real_pair_ff.
 template <bool SLP, bool DLP>
+__device__ __forceinline__ void adj_pair_ff(const RealArgs &a, const AdjWarp &W, int2 e,
+                                            const float2 *tabff, float2 xi2, float2 pf,
+                                            float2 *g)
+{
+    const int t = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
+    const double2 T = a.tp[t];
+    const double2 S = W.pos[slot];
+    const int tbx = a.tbox[t] % a.nx, tby = a.tbox[t] / a.nx;
+    const int ux = tbx - c_nb_dx[k], uy = tby - c_nb_dy[k];
+    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    const float2 x1 = ff_split((S.x - T.x) + zx), x2 = ff_split((S.y - T.y) + zy);
+    const float2 r2 = ff_add(ff_sqr(x1), ff_sqr(x2));
+    const float2 x = ff_mul(r2, xi2);
+    const float2 ex = ff_exp_neg(x, tabff);
+    const float2 ir2 = ff_rcp(r2);
+    const double *wt = a.wcoef + 4 * (int64_t)t;
+    const double *cs = a.coef + (int64_t)a.nc * W.idx[slot];
+    if (SLP && (fl & 1)) {
+        const float2 w1 = ff_split(wt[0]), w2 = ff_split(wt[1]);
+        const float2 f1 = ff_split(cs[0]), f2 = ff_split(cs[1]);
+        const float2 h = ff_scale(ff_mul(ex, ff_g_e1(x, a.gtab)), 0.5f);
+        const float2 gg = ff_mul(ex, ir2);
+        const float2 gq = ff_mul(gg, ff_sub(ff_mul(x1, w2), ff_mul(x2, w1)));
+        g[0] = ff_add(g[0], ff_add(ff_mul(h, w1), ff_mul(gq, x2)));
+        g[1] = ff_add(g[1], ff_sub(ff_mul(h, w2), ff_mul(gq, x1)));
+        const float2 aa = ff_add(ff_mul(x1, w1), ff_mul(x2, w2));
+        const float2 bb = ff_add(ff_mul(x1, f1), ff_mul(x2, f2));
+        const float2 cc = ff_add(ff_mul(w1, f1), ff_mul(w2, f2));
+        const float2 ab = ff_mul(aa, bb);
+        const float2 abr = ff_mul(ab, ir2);
+        // kap = ex (-cc ir2 - 2 xi2 (ab ir2 - cc) - 2 ab ir2^2)
+        float2 kp = ff_neg(ff_mul(cc, ir2));
+        kp = ff_sub(kp, ff_scale(ff_mul(xi2, ff_sub(abr, cc)), 2.0f));
+        kp = ff_sub(kp, ff_scale(ff_mul(abr, ir2), 2.0f));
+        const float2 kap = ff_mul(ex, kp);
+        g[5] = ff_add(g[5], ff_add(ff_mul(kap, x1),
+                                   ff_mul(gg, ff_add(ff_mul(bb, w1), ff_mul(aa, f1)))));
+        g[6] = ff_add(g[6], ff_add(ff_mul(kap, x2),
+                                   ff_mul(gg, ff_add(ff_mul(bb, w2), ff_mul(aa, f2)))));
+    }
+    if (DLP && (fl & 2)) {
+        const float2 w1 = ff_split(wt[2]), w2 = ff_split(wt[3]);
+        const double *Sc = cs + a.doff;
+        const float2 S11 = ff_split(Sc[0]), S1221 = ff_split(Sc[1]), S22 = ff_split(Sc[2]);
+        const float2 ir4 = ff_sqr(ir2);
+        const float2 fb = ff_scale(ff_mul(ff_add_f(x, 1.0f), ir4), -4.0f);
+        const float2 fbp = ff_scale(ff_mul(ff_add_f(x, 2.0f), ff_mul(ir4, ir2)), 4.0f);
+        const float2 wd = ff_add(ff_mul(w1, x1), ff_mul(w2, x2));
+        const float2 fw = ff_mul(fb, wd);
+        const float2 fwx1 = ff_mul(fw, x1), fwx2 = ff_mul(fw, x2);
+        const float2 w1x1 = ff_mul(w1, x1), w2x2 = ff_mul(w2, x2);
+        const float2 w1x2 = ff_mul(w1, x2), w2x1 = ff_mul(w2, x1);
+        // d(w.v)/dS
+        g[2] = ff_add(g[2], ff_mul(ex, ff_add(ff_mul(fwx1, x1),
+                                              ff_mul(pf, ff_add(ff_mul_f(w1x1, 3.0f), w2x2)))));
+        g[3] = ff_add(g[3], ff_mul(ex, ff_add(ff_mul(fwx1, x2), ff_mul(pf, ff_add(w1x2, w2x1)))));
+        g[4] = ff_add(g[4], ff_mul(ex, ff_add(ff_mul(fwx2, x2),
+                                              ff_mul(pf, ff_add(w1x1, ff_mul_f(w2x2, 3.0f))))));
+        // grad_d [w.v(d; S)], subtracted
+        const float2 B11 = ff_add(ff_mul_f(S11, 3.0f), S22), B22 = ff_add(ff_mul_f(S22, 3.0f), S11);
+        const float2 Q = ff_add(ff_add(ff_mul(ff_sqr(x1), S11), ff_mul(ff_mul(x1, x2), S1221)),
+                                ff_mul(ff_sqr(x2), S22));
+        const float2 A1 = ff_add(ff_mul(B11, x1), ff_mul(S1221, x2));
+        const float2 A2 = ff_add(ff_mul(S1221, x1), ff_mul(B22, x2));
+        const float2 wA = ff_add(ff_mul(w1, A1), ff_mul(w2, A2));
+        const float2 Bw1 = ff_add(ff_mul(B11, w1), ff_mul(S1221, w2));
+        const float2 Bw2 = ff_add(ff_mul(S1221, w1), ff_mul(B22, w2));
+        const float2 Sd1 = ff_add(ff_scale(ff_mul(S11, x1), 2.0f), ff_mul(S1221, x2));
+        const float2 Sd2 = ff_add(ff_mul(S1221, x1), ff_scale(ff_mul(S22, x2), 2.0f));
+        const float2 fbQ = ff_mul(fb, Q);
+        const float2 radial = ff_add(ff_scale(ff_mul(xi2, ff_add(ff_mul(fbQ, wd), ff_mul(pf, wA))), -2.0f),
+                                     ff_scale(ff_mul(ff_mul(fbp, Q), wd), 2.0f));
+        const float2 r1 = ff_add(ff_add(ff_mul(radial, x1), ff_mul(fw, Sd1)),
+                                 ff_add(ff_mul(fbQ, w1), ff_mul(pf, Bw1)));
+        const float2 r2b = ff_add(ff_add(ff_mul(radial, x2), ff_mul(fw, Sd2)),
+                                  ff_add(ff_mul(fbQ, w2), ff_mul(pf, Bw2)));
+        g[5] = ff_sub(g[5], ff_mul(ex, r1));
+        g[6] = ff_sub(g[6], ff_mul(ex, r2b));
+    }
+}
+
+template <bool SLP, bool DLP, int FORM>
 __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
 {
+    constexpr bool FF = FORM == kFormFF;
     __shared__ AdjWarp warps[kRealWarps];
     __shared__ double tab[64];
+    __shared__ float2 tabff[64];
     __shared__ double e1s[66];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) tab[i] = c_exp_tab[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+        tab[i] = c_exp_tab[i];
+        tabff[i] = ff_split(c_exp_tab[i]);
+    }
     for (int i = threadIdx.x; i < 66; i += blockDim.x) e1s[i] = (&c_e1[0][0])[i];
     __syncthreads();
-    const float xlo = 1.0f, xhi = INFINITY;   // near FIFO: x <= 1 (all pairs FP64)
+    const float2 xi2ff = ff_split(a.xi2), pfff = ff_split(a.pf);
+    // queue 0: far pairs (float-float in the FF form), queue 1: the rest in FP64
+    const float xlo = FF ? 1.0001f : 1.0f, xhi = FF ? 63.9f : INFINITY;
     AdjWarp &W = warps[wid];
     const int64_t nw = (int64_t)gridDim.x * kRealWarps;
     int head = 0, nfl = 0, gseq = 0;
     int qn[2] = {0, 0}, tag[2] = {-1, -1};
     long long enq[2] = {0, 0}, proc[2] = {0, 0};
     double v[2][kAdjVals];
+    float2 vf[kAdjVals];
+#pragma unroll
+    for (int i = 0; i < kAdjVals; i++) vf[i] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int j = 0; j < 2; j++)
 #pragma unroll
@@ -974,19 +1069,25 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
         int eseq = -1;
         if (e.y >= 0) eseq = gseq - nfl + (((e.y & 0xff) - head + kRing) % kRing);
         const bool fl = tag[j] >= 0 && (lane >= cnt || tag[j] != eseq);
+        const bool ffq = FF && j == 0;
         if (__any_sync(~0u, fl)) {
             double tmp[kAdjVals];
 #pragma unroll
-            for (int i = 0; i < kAdjVals; i++) tmp[i] = fl ? v[j][i] : 0.0;
+            for (int i = 0; i < kAdjVals; i++)
+                tmp[i] = fl ? (ffq ? ff_to_double(vf[i]) : v[j][i]) : 0.0;
             seg_flush_n<kAdjVals>(W.acc, lane, tag[j], tmp);
             if (fl) {
 #pragma unroll
-                for (int i = 0; i < kAdjVals; i++) v[j][i] = 0.0;
+                for (int i = 0; i < kAdjVals; i++) {
+                    v[j][i] = 0.0;
+                    if (ffq) vf[i] = make_float2(0.f, 0.f);   // vf holds queue 0 only
+                }
                 tag[j] = -1;
             }
         }
         if (lane < cnt) {
-            adj_pair<SLP, DLP>(a, W, e, tab, e1s, v[j]);
+            if (ffq) adj_pair_ff<SLP, DLP>(a, W, e, tabff, xi2ff, pfff, vf);
+            else adj_pair<SLP, DLP>(a, W, e, tab, e1s, v[j]);
             tag[j] = eseq;
         }
     };
@@ -1004,9 +1105,19 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
         for (int j = 0; j < 2; j++) {
             batch(j, qn[j]);
             const int key = tag[j] >= 0 ? tag[j] : 0x7fffffff;
-            seg_flush_n<kAdjVals>(W.acc, lane, key, v[j]);
+            if (FF && j == 0) {
+                double tmp[kAdjVals];
 #pragma unroll
-            for (int i = 0; i < kAdjVals; i++) v[j][i] = 0.0;
+                for (int i = 0; i < kAdjVals; i++) tmp[i] = ff_to_double(vf[i]);
+                seg_flush_n<kAdjVals>(W.acc, lane, key, tmp);
+            } else {
+                seg_flush_n<kAdjVals>(W.acc, lane, key, v[j]);
+            }
+#pragma unroll
+            for (int i = 0; i < kAdjVals; i++) {
+                v[j][i] = 0.0;
+                vf[i] = make_float2(0.f, 0.f);
+            }
             tag[j] = -1;
         }
         retire(true);
@@ -1129,9 +1240,12 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
     drain();
 }
 
-template __global__ void k_real_adj<true, false>(RealArgs);
-template __global__ void k_real_adj<false, true>(RealArgs);
-template __global__ void k_real_adj<true, true>(RealArgs);
+template __global__ void k_real_adj<true, false, kFormFP64>(RealArgs);
+template __global__ void k_real_adj<false, true, kFormFP64>(RealArgs);
+template __global__ void k_real_adj<true, true, kFormFP64>(RealArgs);
+template __global__ void k_real_adj<true, false, kFormFF>(RealArgs);
+template __global__ void k_real_adj<false, true, kFormFF>(RealArgs);
+template __global__ void k_real_adj<true, true, kFormFF>(RealArgs);
 
 // ===========================================================================
 // Gaussian spread (fast Gaussian gridding; PE/src/mex/StokesSLP/
@@ -1963,16 +2077,24 @@ cudaError_t launch_sorted_pair(int64_t n, const int *perm, const double2 *a, con
     return cudaGetLastError();
 }
 
+template <int FORM>
+static void launch_real_adj_form(const RealArgs &a, bool slp, bool dlp, unsigned g,
+                                 cudaStream_t st)
+{
+    if (slp && dlp) k_real_adj<true, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+    else if (slp) k_real_adj<true, false, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+    else k_real_adj<false, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+}
+
 cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
-                            int64_t &launches)
+                            int64_t &launches, int form)
 {
     if (a.nouter <= 0) return cudaSuccess;
     const int64_t want = (a.nouter + kRealWarps - 1) / kRealWarps;
     const int64_t cap = (int64_t)sm_count() * 8;
     const unsigned g = (unsigned)(want < cap ? want : cap);
-    if (slp && dlp) k_real_adj<true, true><<<g, kRealWarps * 32, 0, st>>>(a);
-    else if (slp) k_real_adj<true, false><<<g, kRealWarps * 32, 0, st>>>(a);
-    else k_real_adj<false, true><<<g, kRealWarps * 32, 0, st>>>(a);
+    if (form == kFormFF) launch_real_adj_form<kFormFF>(a, slp, dlp, g, st);
+    else launch_real_adj_form<kFormFP64>(a, slp, dlp, g, st);
     launches++;
     return cudaGetLastError();
 }

@@ -96,3 +96,20 @@ def test_ff_composite_agrees_with_native(ft, plans):
     vs, vd = ft.stokes_ewald(p, q, f, g, n, prm, plan=nat)
     assert relerr(us, vs) < FF_VS_NATIVE and relerr(ud, vd) < FF_VS_NATIVE, \
         (relerr(us, vs), relerr(ud, vd))
+
+
+@pytest.mark.parametrize("N,xi,nside,M", [(20000, 120.0, 30, 192), (262144, 430.0, 90, 1344)])
+def test_ff_adjoint_agrees_with_native(ft, plans, N, xi, nside, M):
+    """Dense boxes (~32 points) interleave both pair queues within a source,
+    so queue-0 sums must survive queue-1 flushes."""
+    ff, nat = plans
+    p, q, f, g, n = _cloud(N, 21)
+    rng = np.random.default_rng(22)
+    w1 = rng.standard_normal((2, N))
+    w2 = rng.standard_normal((2, N))
+    prm = ft.EwaldParams.derived(xi, nside, nside, M, M, 24, 1.0, 1.0)
+    a = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm, plan=ff)
+    b = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm, plan=nat)
+    for x, y in zip(a, b):
+        assert relerr(x, y) < 1e-11, relerr(x, y)
+        assert np.max(np.abs(x - y)) <= 1e-11 * np.max(np.abs(y))
