@@ -58,13 +58,18 @@ XI, RC, M, P, L = 860.0, 0.0056, 2688, 24, 1.0
 SEED = 20261203 + 3
 METRIC = "SE Stokes evals/s @1M pts: FP64 tol 1e-10 vs FP32-grid tol 1e-6; fwd+adjoint time"
 UNIT = "evals/s"
-# FP64 FLOPs the fused real-space kernel executes per counted pair (SLP and
-# DLP pairs counted separately, candidate tests included): ncu sass counters
-# 2*DFMA + DMUL + DADD = 16.87 GFLOP over 219.8 M pairs on this workload
-# (profiles/k_real_cfg3.md).  Used only to express the kernel's time as FLOP/s.
-REAL_FP64_FLOP_PER_PAIR = 76.76
-# DRAM bytes (read + write) of one k_real launch on this workload, same capture.
-REAL_DRAM_BYTES = 188.4e6
+# Roofline inputs of the library's own kernels on this workload.  Algorithmic
+# FP64 work per unit: spread (P+1)^2 (1 + 2 C_in) per source with C_in = 5 grids
+# (SLP f1, f2; DLP S11, S12+S21, S22), gather (P+1)^2 (1 + 2 C_out) per target
+# with C_out = 4.  DRAM bytes per launch are ncu's dram__bytes_read + _write of
+# one launch (profiles/).  The real-space kernel of the FP64 form runs its far
+# pairs in float-float on the FP32 pipe; its bound is instruction issue, so its
+# work is the warp instructions ncu counts per accepted pair evaluation.
+C_IN, C_OUT = 5, 4
+SPREAD_FLOP_PER_SOURCE = (P + 1) ** 2 * (1 + 2 * C_IN)
+GATHER_FLOP_PER_TARGET = (P + 1) ** 2 * (1 + 2 * C_OUT)
+DRAM_BYTES = {"spread": 2.878e9, "gather": 0.280e9, "real": 0.364e9}
+REAL_WARP_INST_PER_PAIR = 22.3     # ncu smsp__inst_executed / SLP+DLP pair evaluations
 
 
 def workload(N):
@@ -242,12 +247,12 @@ def fp64_peak_tflops(torch, dev):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
-# Config 4: the mixed-precision workload (same points), tolerance 1e-6.
+# The mixed-precision workload (same points), tolerance 1e-6.
 XI4, RC4, M4, P4 = 860.0, 0.0042, 2048, 12
 
 
 def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
-    """FP32-grid vs FP64 on config 4: evals/s of each, speed-up, and the
+    """FP32-grid vs FP64 on the mixed-precision workload: evals/s of each, speed-up, and the
     FP32-grid error against the FP64 result per potential (max, RMS)."""
     import torch
     import fasttools2d_gb300 as ft
@@ -276,7 +281,7 @@ def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
         a, b = res["fp32_grid"][i], res["fp64"][i]
         err[name] = {"max_rel": float(np.abs(a - b).max() / np.abs(b).max()),
                      "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))}
-    return {"workload": f"config 4: same points, xi={XI4}, rc={RC4} (nside={nside}), M={M4}, "
+    return {"workload": f"SE SLP+DLP, same 1M points, xi={XI4}, rc={RC4} (nside={nside}), M={M4}, "
                         f"P={P4}, tol 1e-6",
             "value": out["fp32_grid"]["evals_per_s"], "unit": UNIT,
             "ms_per_step": out["fp32_grid"]["ms_per_step"],
@@ -285,12 +290,12 @@ def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
             "error_vs_fp64": err}
 
 
-# Config 5: forward + adjoint, N = 2^18.
+# The adjoint workload: forward + adjoint, N = 2^18.
 N5, XI5, RC5, M5, P5 = 2 ** 18, 430.0, 0.011, 1344, 24
 
 
 def adjoint_leg(plan, steps, timed, dev):
-    """Config 5: time of the forward and of forward + adjoint (gradients of
+    """Adjoint workload: time of the forward and of forward + adjoint (gradients of
     J = sum_t w_slp.u_slp + w_dlp.u_dlp w.r.t. source positions, forces,
     densities, normals), and a central-difference check of the gradients on
     16 random coordinates (h = 1e-6, J from the GPU forward)."""
@@ -354,7 +359,7 @@ def adjoint_leg(plan, steps, timed, dev):
         T[a][i, k] = x0
         gi = G[which[a]]
         worst = max(worst, abs((jp - jm) / (2 * h) - gi[i, k]) / np.abs(gi).max())
-    return {"workload": f"config 5: N={N} sources + {N} targets uniform, xi={XI5}, rc={RC5} "
+    return {"workload": f"SE SLP+DLP forward+adjoint, N={N} sources + {N} targets uniform, xi={XI5}, rc={RC5} "
                         f"(nside={nside}), M={M5}, P={P5}, FP64; J = sum_t w.u with w ~ N(0,1)",
             "fwd_ms": t_f, "fwd_adjoint_ms": t_fa, "ratio_fwd_adjoint_over_fwd": t_fa / t_f,
             "fd_check": {"coords": 16, "h": h, "max_err_rel_to_max_grad": worst}}
@@ -470,32 +475,48 @@ def gpu_arm(args, rank, world, local_rank):
     plan.enable_timing(False)
     plan.set_overlap(True)
 
-    # ---- FP32-grid form (config 4) next to the FP64 form on the same workload
+    # ---- FP32-grid form (mixed-precision workload) next to the FP64 form on the same workload
     legs = set(args.legs.split(","))
     mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev) \
         if "fp32_grid" in legs else None
     adjoint = adjoint_leg(plan, args.steps, timed, dev) if "adjoint" in legs else None
 
     # ---- roofline of the dominant kernel ---------------------------------
+    # Stage times come from CUDA events on each kernel's own stream, taken in
+    # the serialised pass above; the top one among this library's kernels
+    # (cuFFT excluded) gets the roofline.
     kstages = {k: v for k, v in stages.items() if k not in ("h2d", "d2h") and v[1] > 0}
-    top = max(kstages, key=lambda k: kstages[k][0])
-    top_ms = kstages[top][0] / kstages[top][1]
-    peak = fp64_peak_tflops(torch, dev)
+    per = {k: v[0] / v[1] for k, v in kstages.items()}
+    own = {k: per[k] for k in ("real", "spread", "gather", "filter") if k in per}
+    top = max(own, key=own.get)
+    top_ms = own[top]
     pairs_per_launch = (counts[1] + counts[2]) / args.steps     # counted in the timed region
-    real_ms = kstages["real"][0] / kstages["real"][1] if "real" in kstages else float("nan")
-    real_flops = pairs_per_launch * REAL_FP64_FLOP_PER_PAIR
-    roof = {"kernel": "k_real (fused SLP+DLP real-space pair sum)", "bound": "fp64",
-            "achieved": real_flops / (real_ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
-            "peak_source": "cuBLAS DGEMM 2048^3 measured in this run "
-                           "(MEASURED_PEAKS.json holds no FP64 figure)",
-            "traffic": REAL_DRAM_BYTES, "traffic_unit": "bytes/launch (ncu)",
-            "ms_per_launch": real_ms,
-            "accepted_pairs_per_launch": pairs_per_launch,
-            "candidates_per_launch": counts[0] / args.steps,
-            "pairs_per_s": pairs_per_launch / (real_ms * 1e-3),
-            "flop_per_pair": REAL_FP64_FLOP_PER_PAIR, "top_stage": top,
-            "top_stage_ms": top_ms}
-    roof["frac"] = roof["achieved"] / roof["peak"]
+    evals_per_launch = pairs_per_launch / 2                     # SLP and DLP share each evaluation
+    clock_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    if top == "real":
+        achieved = evals_per_launch * REAL_WARP_INST_PER_PAIR / (top_ms * 1e-3) / 1e12
+        roof = {"kernel": "k_real<SLP,DLP,float-float> (fused real-space pair sum)",
+                "bound": "issue", "achieved": achieved,
+                "peak": 4 * sms * clock_ghz * 1e9 / 1e12, "unit": "T warp-inst/s",
+                "peak_source": "4 warp instructions per clock per SM x SMs x measured SM clock"}
+    else:
+        flops = (N * SPREAD_FLOP_PER_SOURCE if top == "spread" else N * GATHER_FLOP_PER_TARGET)
+        roof = {"kernel": {"spread": "k_spread<5> (Gaussian spread, 5 grids)",
+                           "gather": "k_gather<4,24> (Gaussian gather, 4 grids)",
+                           "filter": "k_filter"}[top],
+                "bound": "fp64", "achieved": flops / (top_ms * 1e-3) / 1e12,
+                "peak": fp64_peak_tflops(torch, dev), "unit": "TFLOP/s",
+                "peak_source": "cuBLAS DGEMM 2048^3 measured in this run "
+                               "(MEASURED_PEAKS.json holds no FP64 figure)"}
+    roof.update({"frac": roof["achieved"] / roof["peak"],
+                 "traffic": DRAM_BYTES.get(top), "traffic_unit": "bytes/launch (ncu)",
+                 "ms_per_launch": top_ms, "top_stage": top,
+                 "real_space": {"ms_per_launch": per.get("real"),
+                                "accepted_pairs_per_launch": pairs_per_launch,
+                                "candidates_per_launch": counts[0] / args.steps,
+                                "pairs_per_s": pairs_per_launch / (per["real"] * 1e-3)
+                                if "real" in per else None}})
     stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1] > 0}
 
     line = {

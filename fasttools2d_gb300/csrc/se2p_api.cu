@@ -64,7 +64,8 @@ struct se2p_plan_st {
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;     // real space runs here, concurrently with k space
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t kst = nullptr;      // k space beside real space (highest priority)
+    cudaEvent_t fork = nullptr, join = nullptr, kjoin = nullptr;
     std::string err;
     int64_t launches = 0;
     DevBuf buf[S_COUNT_SLOTS];
@@ -160,6 +161,7 @@ int ensure(se2p_plan pl, int slot, size_t bytes, void **out)
         if (b.p) {
             CK(cudaStreamSynchronize(pl->stream));
             if (pl->side) CK(cudaStreamSynchronize(pl->side));
+            if (pl->kst) CK(cudaStreamSynchronize(pl->kst));
             CK(cudaFree(b.p));
             b.p = nullptr;
             b.bytes = 0;
@@ -256,13 +258,13 @@ int finish_out(se2p_plan pl, const OutBuf &o)
 }
 
 // dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32)
-int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
+int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, cufftHandle *h)
 {
     auto key = std::make_tuple(Mx, My, batch, dir);
     auto it = pl->ffts.find(key);
     if (it != pl->ffts.end()) {
         *h = it->second;
-        CKF(cufftSetStream(*h, pl->stream));
+        CKF(cufftSetStream(*h, st));
         return SE2P_OK;
     }
     int n[2] = {Mx, My};
@@ -274,7 +276,7 @@ int get_fft(se2p_plan pl, int Mx, int My, int batch, int dir, cufftHandle *h)
         CKF(cufftPlanMany(&p, 2, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, type, batch));
     else
         CKF(cufftPlanMany(&p, 2, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, type, batch));
-    CKF(cufftSetStream(p, pl->stream));
+    CKF(cufftSetStream(p, st));
     pl->ffts[key] = p;
     *h = p;
     return SE2P_OK;
@@ -637,6 +639,14 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         if (side) CK(cudaEventRecord(pl->join, rs));
     }
 
+    // The k-space chain runs on a high-priority plan stream when real space
+    // runs beside it, so its (FP64-bound) kernels take SMs first and the real
+    // space fills the remaining issue slots.
+    cudaStream_t ks = st;
+    if (J.real && J.kspace && pl->overlap) {
+        ks = pl->kst;
+        CK(cudaStreamWaitEvent(ks, pl->fork, 0));
+    }
     if (J.kspace && pl->precision == SE2P_PRECISION_FP32_GRID) {
         // FP32-grid form: spread, FFT, filter and gather in FP32 (se2p_kernels_f32.cu)
         const int Mx = J.Mx, My = J.My, P = J.P;
@@ -648,17 +658,17 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         CKS(ensure_t(pl, S_GRID, G * nc, &grid));
         CKS(ensure_t(pl, S_SPEC, H * nc, &spec));
         CKS(ensure_t(pl, S_UK, ntz * (nout / 2), &uk));
-        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G * nc, st));
+        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G * nc, ks));
         SpreadArgsF sa{sp, coef, ns, grid, Mx, My, P, J.Lx / 2.0, J.Ly / 2.0, h, J.w,
                        -2 * J.xi * J.xi / J.eta};
         {
-            StageTimer tm(pl, T_SPREAD);
-            CK(launch_spread_f32(sa, nc, sm_count(), st, pl->launches));
+            StageTimer tm(pl, T_SPREAD, ks);
+            CK(launch_spread_f32(sa, nc, sm_count(), ks, pl->launches));
         }
         cufftHandle fwd, inv;
-        CKS(get_fft(pl, Mx, My, nc, 2, &fwd));
+        CKS(get_fft(pl, ks, Mx, My, nc, 2, &fwd));
         {
-            StageTimer tm(pl, T_FFT_FWD);
+            StageTimer tm(pl, T_FFT_FWD, ks);
             CKF(cufftExecR2C(fwd, grid, spec));
         }
         FilterArgsF fa;
@@ -675,20 +685,20 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.slp_out = 0;
         fa.dlp_out = J.slp ? 2 : 0;
         {
-            StageTimer tm(pl, T_FILTER);
-            CK(launch_filter_f32(fa, st, pl->launches));
+            StageTimer tm(pl, T_FILTER, ks);
+            CK(launch_filter_f32(fa, ks, pl->launches));
         }
-        CKS(get_fft(pl, Mx, My, nout, 3, &inv));
+        CKS(get_fft(pl, ks, Mx, My, nout, 3, &inv));
         {
-            StageTimer tm(pl, T_FFT_INV);
+            StageTimer tm(pl, T_FFT_INV, ks);
             CKF(cufftExecC2R(inv, spec, grid));
         }
         double s = 4 * J.xi * J.xi / J.eta;               // mex_stokes_slp_kspace.cpp:325-328
         s = s * s * h * h / kPi;
         GatherArgsF ga{tp, nt, grid, Mx, My, P, J.Lx / 2.0, J.Ly / 2.0, h, J.w,
                        -2 * J.xi * J.xi / J.eta, s / (4 * kPi), uk};
-        StageTimer tm(pl, T_GATHER);
-        CK(launch_gather_f32(ga, nout, st, pl->launches));
+        StageTimer tm(pl, T_GATHER, ks);
+        CK(launch_gather_f32(ga, nout, ks, pl->launches));
     } else if (J.kspace) {
         const int Mx = J.Mx, My = J.My, P = J.P;
         const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
@@ -704,8 +714,8 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         double e1h[kMaxP + 1];
         const double t = -2 * J.xi * J.xi / J.eta * h * h;
         for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
-        CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, st));
-        CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * nc, st));
+        CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, ks));
+        CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * nc, ks));
 
         SpreadArgs sa;
         sa.sp = sp;
@@ -722,14 +732,14 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         sa.a = -2 * J.xi * J.xi / J.eta;
         sa.e1 = e1;
         {
-            StageTimer tm(pl, T_SPREAD);
-            CK(launch_spread(sa, nc, st, pl->launches));
+            StageTimer tm(pl, T_SPREAD, ks);
+            CK(launch_spread(sa, nc, ks, pl->launches));
         }
 
         cufftHandle fwd, inv;
-        CKS(get_fft(pl, Mx, My, nc, 0, &fwd));
+        CKS(get_fft(pl, ks, Mx, My, nc, 0, &fwd));
         {
-            StageTimer tm(pl, T_FFT_FWD);
+            StageTimer tm(pl, T_FFT_FWD, ks);
             CKF(cufftExecD2Z(fwd, grid, spec));
         }
 
@@ -748,14 +758,14 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.dlp_out = J.slp ? 2 : 0;
         fa.etab = nullptr;
         {
-            StageTimer tm(pl, T_FILTER);
-            CKS(filter_table(pl, fa, st));
-            CK(launch_filter(fa, st, pl->launches));
+            StageTimer tm(pl, T_FILTER, ks);
+            CKS(filter_table(pl, fa, ks));
+            CK(launch_filter(fa, ks, pl->launches));
         }
 
-        CKS(get_fft(pl, Mx, My, nout, 1, &inv));
+        CKS(get_fft(pl, ks, Mx, My, nout, 1, &inv));
         {
-            StageTimer tm(pl, T_FFT_INV);
+            StageTimer tm(pl, T_FFT_INV, ks);
             CKF(cufftExecZ2D(inv, spec, grid));
         }
 
@@ -776,8 +786,13 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ga.scale = s / (4 * kPi);
         ga.e1 = e1;
         ga.out = uk;
-        StageTimer tm(pl, T_GATHER);
-        CK(launch_gather(ga, nout, st, pl->launches));
+        StageTimer tm(pl, T_GATHER, ks);
+        CK(launch_gather(ga, nout, ks, pl->launches));
+    }
+
+    if (ks != st) {
+        CK(cudaEventRecord(pl->kjoin, ks));
+        CK(cudaStreamWaitEvent(st, pl->kjoin, 0));
     }
 
     double2 *zm = nullptr;
@@ -951,6 +966,12 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     }
     if (side) CK(cudaEventRecord(pl->join, rs));
 
+    // k space on the high-priority plan stream beside the real space
+    cudaStream_t ks = st;
+    if (side) {
+        ks = pl->kst;
+        CK(cudaStreamWaitEvent(ks, pl->fork, 0));
+    }
     // ... k space: spread w at the targets, D2Z, adjoint filter, Z2D, gather
     // with weight gradients at the sources.
     const int Mx = J.Mx, My = J.My, P = J.P;
@@ -964,8 +985,8 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     double e1h[kMaxP + 1];
     const double t = -2 * J.xi * J.xi / J.eta * h * h;
     for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
-    CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * 4, st));
+    CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, ks));
+    CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * 4, ks));
     SpreadArgs sa;
     sa.sp = tp;
     sa.coef = wcoef;
@@ -981,13 +1002,13 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     sa.a = -2 * J.xi * J.xi / J.eta;
     sa.e1 = e1;
     {
-        StageTimer tm(pl, T_SPREAD);
-        CK(launch_spread(sa, 4, st, pl->launches));
+        StageTimer tm(pl, T_SPREAD, ks);
+        CK(launch_spread(sa, 4, ks, pl->launches));
     }
     cufftHandle fwd, inv;
-    CKS(get_fft(pl, Mx, My, 4, 0, &fwd));
+    CKS(get_fft(pl, ks, Mx, My, 4, 0, &fwd));
     {
-        StageTimer tm(pl, T_FFT_FWD);
+        StageTimer tm(pl, T_FFT_FWD, ks);
         CKF(cufftExecD2Z(fwd, grid, spec));
     }
     FilterArgs fa;
@@ -1005,13 +1026,13 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     fa.dlp_out = 2;
     fa.etab = nullptr;
     {
-        StageTimer tm(pl, T_FILTER);
-        CKS(filter_table(pl, fa, st));
-        CK(launch_filter_adj(fa, st, pl->launches));
+        StageTimer tm(pl, T_FILTER, ks);
+        CKS(filter_table(pl, fa, ks));
+        CK(launch_filter_adj(fa, ks, pl->launches));
     }
-    CKS(get_fft(pl, Mx, My, 5, 1, &inv));
+    CKS(get_fft(pl, ks, Mx, My, 5, 1, &inv));
     {
-        StageTimer tm(pl, T_FFT_INV);
+        StageTimer tm(pl, T_FFT_INV, ks);
         CKF(cufftExecZ2D(inv, spec, grid));
     }
     GatherAdjArgs ga;
@@ -1033,8 +1054,12 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     ga.e1 = e1;
     ga.out = gk;
     {
-        StageTimer tm(pl, T_GATHER);
-        CK(launch_gather_adj(ga, st, pl->launches));
+        StageTimer tm(pl, T_GATHER, ks);
+        CK(launch_gather_adj(ga, ks, pl->launches));
+    }
+    if (ks != st) {
+        CK(cudaEventRecord(pl->kjoin, ks));
+        CK(cudaStreamWaitEvent(st, pl->kjoin, 0));
     }
     if (side) CK(cudaStreamWaitEvent(st, pl->join, 0));
 
@@ -1082,9 +1107,13 @@ int se2p_plan_create(se2p_plan *plan, int device)
         return SE2P_ERR_CUDA;
     }
     pl->stream = pl->own;
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
     if (cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&pl->kst, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->kjoin, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         se2p_plan_destroy(pl);
         return SE2P_ERR_CUDA;
@@ -1098,6 +1127,8 @@ int se2p_plan_destroy(se2p_plan pl)
     if (!pl) return SE2P_OK;
     DeviceGuard guard(pl->device);
     cudaStreamSynchronize(pl->stream);
+    if (pl->side) cudaStreamSynchronize(pl->side);
+    if (pl->kst) cudaStreamSynchronize(pl->kst);
     for (auto &v : pl->pending)
         for (auto &ev : v) {
             cudaEventDestroy(ev.first);
@@ -1110,8 +1141,13 @@ int se2p_plan_destroy(se2p_plan pl)
         cudaStreamSynchronize(pl->side);
         cudaStreamDestroy(pl->side);
     }
+    if (pl->kst) {
+        cudaStreamSynchronize(pl->kst);
+        cudaStreamDestroy(pl->kst);
+    }
     if (pl->fork) cudaEventDestroy(pl->fork);
     if (pl->join) cudaEventDestroy(pl->join);
+    if (pl->kjoin) cudaEventDestroy(pl->kjoin);
     if (pl->own) cudaStreamDestroy(pl->own);
     delete pl;
     return SE2P_OK;

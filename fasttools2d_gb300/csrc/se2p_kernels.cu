@@ -306,6 +306,7 @@ struct RealWarp {
     int2 q[2][64];              // pair FIFOs: [0] main, [1] near field (x <= 1)
                                 // entry = (sorted source, slot | k << 8 | flags << 12)
     double acc[kRing][4];       // per-target sums: SLP u1, u2, DLP u1, u2
+    float2 accf[kRing][4];      // the same from float-float pairs (FP64 form, queue 0)
     double2 tpos[kRing];
     int tbox[kRing];
     long long tidx[kRing];
@@ -333,6 +334,31 @@ __device__ __forceinline__ void seg_flush(RealWarp &W, int lane, int key, double
     if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
         double *a = W.acc[key % kRing];
         a[0] += v0; a[1] += v1; a[2] += v2; a[3] += v3;
+    }
+    __syncwarp();
+}
+
+// seg_flush for float-float sums (queue 0 of the FP64 form), into W.accf.
+__device__ __forceinline__ void seg_flush_ff(RealWarp &W, int lane, int key, float2 v0, float2 v1,
+                                             float2 v2, float2 v3)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ko = __shfl_up_sync(~0u, key, o);
+        float2 a0, a1, a2, a3;
+        a0.x = __shfl_up_sync(~0u, v0.x, o); a0.y = __shfl_up_sync(~0u, v0.y, o);
+        a1.x = __shfl_up_sync(~0u, v1.x, o); a1.y = __shfl_up_sync(~0u, v1.y, o);
+        a2.x = __shfl_up_sync(~0u, v2.x, o); a2.y = __shfl_up_sync(~0u, v2.y, o);
+        a3.x = __shfl_up_sync(~0u, v3.x, o); a3.y = __shfl_up_sync(~0u, v3.y, o);
+        if (lane >= o && ko == key) {
+            v0 = ff_add(v0, a0); v1 = ff_add(v1, a1); v2 = ff_add(v2, a2); v3 = ff_add(v3, a3);
+        }
+    }
+    const int kn = __shfl_down_sync(~0u, key, 1);
+    if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
+        float2 *a = W.accf[key % kRing];
+        a[0] = ff_add(a[0], v0); a[1] = ff_add(a[1], v1);
+        a[2] = ff_add(a[2], v2); a[3] = ff_add(a[3], v3);
     }
     __syncwarp();
 }
@@ -444,16 +470,21 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
     const double2 T = W.tpos[slot];
     const int tb = W.tbox[slot];
     const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
-    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
-    const float x1 = (float)((S.x - T.x) + zx), x2 = (float)((S.y - T.y) + zy);
-    const float dxs = (float)(S.x - (T.x - zx)), dys = (float)(S.y - (T.y - zy));
+    // one FP64 offset (a second add only across a periodic image), rounded to
+    // FP32 through the bit-pattern split (conversions run at the FP64 rate)
+    double dx = S.x - T.x, dy = S.y - T.y;
+    if (ux < 0 || ux >= a.nx || uy < 0 || uy >= a.ny) {
+        dx += ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+        dy += uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    }
+    const float x1 = ff_split(dx).x, x2 = ff_split(dy).x;
+    const float dxs = x1, dys = x2;
     const float xi2 = a.xi2f;
     if (SLP && (fl & 1)) {
         const float r2 = fmaf(dxs, dxs, dys * dys);
         const float x = r2 * xi2;
         const float ex = __expf(-x);
-        const float ir2 = 1.0f / r2;
+        const float ir2 = __frcp_rn(r2);
         const int set = x >= 16.f ? 0 : (x > 1.f ? 1 : 2);
         const float *c = e1f + 22 * set;
         const float z = set == 2 ? x : ir2 * (float)a.inv_xi2;
@@ -463,8 +494,8 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
             pa = fmaf(z, pa, c[i]);
             pb = fmaf(z, pb, c[i + 1]);
         }
-        const float E = set == 2 ? pa / pb + x - __logf(x) - 0.66373538970947265625f
-                                 : ex * (z + pa / (pb + x));
+        const float E = set == 2 ? __fdividef(pa, pb) + x - __logf(x) - 0.66373538970947265625f
+                                 : ex * (z + __fdividef(pa, pb + x));
         const float f1 = (float)a.coef[(int64_t)a.nc * s], f2 = (float)a.coef[(int64_t)a.nc * s + 1];
         const float h = 0.5f * E, gq = ex * ir2 * fmaf(dxs, f2, -dys * f1);
         s1 = fmaf(h, f1, fmaf(gq, dys, s1));
@@ -476,7 +507,7 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
         const float r2 = fmaf(x1, x1, x2 * x2);
         const float x = r2 * xi2;
         const float ex = __expf(-x);
-        const float ir2 = 1.0f / r2;
+        const float ir2 = __frcp_rn(r2);
         const float fb = -4.f * (1.f + x) * ir2 * ir2;
         const float Q = fmaf(x1 * x1, S11, fmaf(x1 * x2, S1221, x2 * x2 * S22));
         const float A1 = fmaf(x1, fmaf(3.f, S11, S22), x2 * S1221);
@@ -528,9 +559,12 @@ __device__ __forceinline__ void real_pair_ff(const RealArgs &a, const RealWarp &
     // image shift of neighbour k of this pair's target (the FIFO outlives W.nbz)
     const int tb = W.tbox[slot];
     const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
-    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
-    const float2 x1 = ff_split((S.x - T.x) + zx), x2 = ff_split((S.y - T.y) + zy);
+    double dx = S.x - T.x, dy = S.y - T.y;
+    if (ux < 0 || ux >= a.nx || uy < 0 || uy >= a.ny) {   // across a periodic image
+        dx += ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+        dy += uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    }
+    const float2 x1 = ff_split(dx), x2 = ff_split(dy);
     const float2 r2 = ff_add(ff_sqr(x1), ff_sqr(x2));
     const float2 x = ff_mul(r2, xi2);
     const float2 ex = ff_exp_neg(x, tabff);
@@ -619,15 +653,18 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         const bool f32 = MIXED && j == 0;
         const bool ffp = FF && j == 0;
         if (__any_sync(~0u, fl)) {
-            double v0 = P.s1, v1 = P.s2, v2 = P.d1, v3 = P.d2;
-            if (f32) {
-                v0 = (double)P.f1; v1 = (double)P.f2; v2 = (double)P.g1; v3 = (double)P.g2;
-            }
+            const float2 z = make_float2(0.f, 0.f);
             if (ffp) {
-                v0 = ff_to_double(P.h1); v1 = ff_to_double(P.h2);
-                v2 = ff_to_double(P.k1); v3 = ff_to_double(P.k2);
+                seg_flush_ff(W, lane, P.tag, fl ? P.h1 : z, fl ? P.h2 : z, fl ? P.k1 : z,
+                             fl ? P.k2 : z);
+            } else if (f32) {
+                seg_flush_ff(W, lane, P.tag, make_float2(fl ? P.f1 : 0.f, 0.f),
+                             make_float2(fl ? P.f2 : 0.f, 0.f), make_float2(fl ? P.g1 : 0.f, 0.f),
+                             make_float2(fl ? P.g2 : 0.f, 0.f));
+            } else {
+                seg_flush(W, lane, P.tag, fl ? P.s1 : 0.0, fl ? P.s2 : 0.0, fl ? P.d1 : 0.0,
+                          fl ? P.d2 : 0.0);
             }
-            seg_flush(W, lane, P.tag, fl ? v0 : 0.0, fl ? v1 : 0.0, fl ? v2 : 0.0, fl ? v3 : 0.0);
             if (fl) {
                 P.s1 = P.s2 = P.d1 = P.d2 = 0.0;
                 P.f1 = P.f2 = P.g1 = P.g2 = 0.f;
@@ -647,10 +684,12 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
     auto retire = [&](bool all) {
         while (nfl > 0 && (all || (Q[0].proc >= W.tend[0][head] + 32 &&
                                    Q[1].proc >= W.tend[1][head] + 32))) {
-            if (lane == 0) {
+            if (lane < 4 && (lane < 2 ? SLP : DLP)) {
                 const long long t = W.tidx[head];
-                if (SLP) a.u_slp[t] = make_double2(W.acc[head][0], W.acc[head][1]);
-                if (DLP) a.u_dlp[t] = make_double2(W.acc[head][2], W.acc[head][3]);
+                double v = W.acc[head][lane];
+                if (FF || MIXED) v += ff_to_double(W.accf[head][lane]);
+                double *u = reinterpret_cast<double *>(lane < 2 ? a.u_slp : a.u_dlp);
+                u[2 * t + (lane & 1)] = v;
             }
             head = (head + 1) % kRing;
             nfl--;
@@ -663,11 +702,10 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
             batch(j, Q[j].qn);
             const int key = Q[j].tag >= 0 ? Q[j].tag : 0x7fffffff;
             if (MIXED && j == 0)
-                seg_flush(W, lane, key, (double)Q[j].f1, (double)Q[j].f2, (double)Q[j].g1,
-                          (double)Q[j].g2);
+                seg_flush_ff(W, lane, key, make_float2(Q[j].f1, 0.f), make_float2(Q[j].f2, 0.f),
+                             make_float2(Q[j].g1, 0.f), make_float2(Q[j].g2, 0.f));
             else if (FF && j == 0)
-                seg_flush(W, lane, key, ff_to_double(Q[j].h1), ff_to_double(Q[j].h2),
-                          ff_to_double(Q[j].k1), ff_to_double(Q[j].k2));
+                seg_flush_ff(W, lane, key, Q[j].h1, Q[j].h2, Q[j].k1, Q[j].k2);
             else
                 seg_flush(W, lane, key, Q[j].s1, Q[j].s2, Q[j].d1, Q[j].d2);
             Q[j].s1 = Q[j].s2 = Q[j].d1 = Q[j].d2 = 0.0;
@@ -686,7 +724,10 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         const int tb = a.tbox[t];
         const double2 T = a.tp[t];
         const float2 Tf = a.tpf[t];
-        if (lane < 4) W.acc[slot][lane] = 0.0;
+        if (lane < 4) {
+            W.acc[slot][lane] = 0.0;
+            W.accf[slot][lane] = make_float2(0.f, 0.f);
+        }
         if (lane == 0) {
             W.tpos[slot] = T;
             W.tbox[slot] = tb;
@@ -725,10 +766,21 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                 while (v >= W.nbp[k + 1]) k++;
                 s = W.nbs[k] + (v - W.nbp[k]);
                 if (k == 0) {
-                    const double2 S = a.sp[s];
-                    const double dx = xsub(T.x, S.x), dy = xsub(T.y, S.y);
-                    const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
-                    if (r2 == 0.0) {
+                    // own box, no cutoff.  Distinct FP32 images imply an FP64
+                    // r2 > 0 (the offset is then >= 2^-150, its square normal),
+                    // so only r2f == 0 (or NaN) needs the reference's exact r2.
+                    const float2 Sf = a.spf[s];
+                    const float dxf = Tf.x - Sf.x, dyf = Tf.y - Sf.y;
+                    float r2f = dxf * dxf + dyf * dyf;
+                    bool self = false;
+                    if (!(r2f > 0.0f)) {
+                        const double2 S = a.sp[s];
+                        const double dx = xsub(T.x, S.x), dy = xsub(T.y, S.y);
+                        const double r2 = xadd(xmul(dx, dx), xmul(dy, dy));
+                        self = r2 == 0.0;
+                        r2f = (float)r2;
+                    }
+                    if (self) {
                         // SLP self term (mex_stokes_slp_real.cpp:161-163); DLP skips r2 == 0.
                         if (SLP) {
                             const double *f = a.coef + (int64_t)a.nc * s;
@@ -737,7 +789,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
                         }
                     } else {
                         fl = 3;
-                        const float xf = (float)r2 * a.xi2f;
+                        const float xf = r2f * a.xi2f;
                         nearp = !(xf > xlo && xf < xhi);
                     }
                 } else {
@@ -1979,7 +2031,9 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
 {
     if (a.ntar <= 0) return cudaSuccess;
     const int64_t want = (a.ntar + kRealWarps - 1) / kRealWarps;
-    const int64_t cap = (int64_t)sm_count() * 8;
+    // At most 4 resident-sized waves: the k-space chain (high-priority stream)
+    // keeps SMs for itself while real space fills the remaining issue slots.
+    const int64_t cap = (int64_t)sm_count() * 4;
     const unsigned g = (unsigned)(want < cap ? want : cap);
     if (form == kFormF32) launch_real_form<kFormF32>(a, slp, dlp, g, st);
     else if (form == kFormFF) launch_real_form<kFormFF>(a, slp, dlp, g, st);

@@ -123,16 +123,16 @@ def targets_outside(rng, nt, cs, L=1.0):
 
 def main():
     R = ref_mex.RefMex()
-    # Config 1: SLP FP64, N=1000, targets = sources (the self term enters at r2 == 0).
-    uniform_case(R, "cfg1", SEED0 + 1, 1000, 19.2, 4, 64, 24, targets_are_sources=True,
+    # SLP FP64, N=1000, targets = sources (the self term enters at r2 == 0).
+    uniform_case(R, "slp1000_xi19", SEED0 + 1, 1000, 19.2, 4, 64, 24, targets_are_sources=True,
                  with_direct=True)
 
-    # Config 2 geometry at reduced size: 8 circles x 256 points, 2048 targets outside.
+    # Circle geometry at reduced size: 8 circles x 256 points, 2048 targets outside.
     rng = np.random.default_rng(SEED0 + 2)
     ps, f, n, cs = circles(rng, 8, 256)
     pt = targets_outside(rng, 2048, cs)
     prm = mex_params(60.0, 12, 12, 192, 192, 1.0, 1.0, 24)
-    _save("cfg2_small", ps, pt, f, n, prm, _run_ref(R, ps, pt, f, n, prm))
+    _save("circles2048_xi60", ps, pt, f, n, prm, _run_ref(R, ps, pt, f, n, prm))
 
     # direct_sums_test.m layout: N=10, Lx=1, Ly=2, driver parameters at tol=1e-16
     # (PE/tests/direct_sums_test.m:13-38), separate SLP and DLP parameter sets.

@@ -3,7 +3,7 @@
 J = sum_t w_slp(t).u_slp(t) + w_dlp(t).u_dlp(t).  The hand-written adjoint
 gradients with respect to source positions, SLP forces, DLP densities and
 normals are compared with central finite differences (h = 1e-6) of J, computed
-(a) with the GPU forward, at small and at config-5 size, and (b) with the CPU
+(a) with the GPU forward, at small size and at N = 2^18, and (b) with the CPU
 oracle (the reference's algorithm) evaluated on perturbed inputs.  Parameters
 keep the real-space truncation jumps small (xi^2 rc^2 well above 20), so a
 pair crossing the cutoff within +-h cannot spoil the differences.
@@ -88,8 +88,8 @@ def test_adjoint_vs_reference_on_perturbed_inputs(ft):
     plan.close()
 
 
-def test_adjoint_config5_size(ft):
-    """Config 5: N = 262,144, xi = 430, rc = 0.011 (nside 90), M = 1344, P = 24,
+def test_adjoint_262144_points(ft):
+    """N = 262,144, xi = 430, rc = 0.011 (nside 90), M = 1344, P = 24,
     64 random coordinates, GPU forward for J."""
     torch = pytest.importorskip("torch")
     N = 262144

@@ -35,7 +35,7 @@ def ft():
 
 
 def test_fp32grid_vs_fp64_oracle(ft):
-    """Config-4-like (xi rc = 3.61, P = 12) at N = 2^15 against the oracle."""
+    """xi rc = 3.61, P = 12 (the 1M-point mixed-precision workload's ratios) at N = 2^15 against the oracle."""
     from oracle import oracle as O
     N = 2 ** 15
     p, q, f, g, n = _inputs(N, 17)
@@ -57,7 +57,7 @@ def test_fp32grid_vs_fp64_oracle(ft):
 def test_fp32grid_mex_gateways(ft, kind):
     """Each gateway in FP32-grid mode stays within the FP32 error budget."""
     from conftest import load_golden
-    g = load_golden("cfg1")
+    g = load_golden("slp1000_xi19")
     ps, f, n = g["psrc"], g["f"], g["n"]
     plan = ft.Plan(0)
     plan.set_precision("fp32_grid")

@@ -83,9 +83,9 @@ def test_rectangular_driver(ft, plan):
     assert relerr(ud, O.dlp_ewald(p, p, f, n, 14.0, 3, 6, 40, 80, 1.0, 2.0, 24)[0]) < PARITY
 
 
-def test_cfg1_meets_ewald_tolerance(ft, plan):
-    """Config 1 (xi=19.2, rc=0.25, M=64, P=24) against the FP64 direct lattice sum."""
-    g = load_golden("cfg1")
+def test_slp1000_meets_ewald_tolerance(ft, plan):
+    """SLP, 1000 points (xi=19.2, rc=0.25, M=64, P=24) against the FP64 direct lattice sum."""
+    g = load_golden("slp1000_xi19")
     ps, f = g["psrc"], g["f"]
     u = ft.mex_stokes_slp_real(ps, ps, f, g["xi"], 4, 4, 1.0, 1.0, plan=plan) + \
         ft.mex_stokes_slp_kspace(ps, ps, g["xi"], g["eta"], f, 64, 64, 1.0, 1.0, g["w"], 24,
@@ -94,8 +94,8 @@ def test_cfg1_meets_ewald_tolerance(ft, plan):
     assert relerr(u, ds) < 1e-10
 
 
-def test_cfg2_circles_full_size(ft, plan):
-    """Config 2: 8 circles x 8192 points (65,536 DLP sources), 65,536 targets
+def test_circles_full_size(ft, plan):
+    """8 circles x 8192 points (65,536 DLP sources), 65,536 targets
     outside the circles, xi=60, rc=0.08 (nside 12), M=192, P=24."""
     from oracle import oracle as O
     from tests.golden.make_golden import circles, targets_outside
@@ -159,7 +159,7 @@ def test_argument_errors(ft, plan):
     with pytest.raises(ValueError):          # MEX shape check
         ft.mex_stokes_dlp_real(p, p, np.zeros((2, 3)), p, 10.0, 4, 4, 1.0, 1.0, plan=plan)
     # the plan stays usable after errors
-    g = load_golden("cfg1")
+    g = load_golden("slp1000_xi19")
     u = ft.mex_stokes_slp_real(g["psrc"], g["ptar"], g["f"], g["xi"], 4, 4, 1.0, 1.0, plan=plan)
     assert relerr(u, g["out_slp_real"]) < PARITY
 

@@ -89,7 +89,7 @@ def test_gateways_match_reference(gw, name):
 
 @pytest.mark.gpu
 def test_gateways_plan_reuse_and_clear(gw):
-    d = load_golden("cfg1")
+    d = load_golden("slp1000_xi19")
     a = gw.call("mex_stokes_slp_real", *_args(d, "slp_real"))
     b = gw.call("mex_stokes_slp_real", *_args(d, "slp_real"))
     assert relerr(a, b) <= 1e-13
@@ -100,7 +100,7 @@ def test_gateways_plan_reuse_and_clear(gw):
 
 @pytest.mark.gpu
 def test_gateways_empty_targets(gw):
-    d = load_golden("cfg1")
+    d = load_golden("slp1000_xi19")
     for kind in KINDS:
         a = list(_args(d, kind))
         a[1] = np.zeros((2, 0))

@@ -72,9 +72,9 @@ def test_reference_vs_direct_sums(golden, kind):
     assert relerr(ks, g[f"out_{kind}_kspace_ds"]) < 1e-12
 
 
-def test_cfg1_total_vs_direct_lattice_sum(golden):
-    """Config 1 SLP at xi=19.2, rc=0.25, M=64, P=24 meets its ~1e-10 tolerance."""
-    g = golden("cfg1")
+def test_slp1000_total_vs_direct_lattice_sum(golden):
+    """SLP, 1000 points, xi=19.2, rc=0.25, M=64, P=24 meets its ~1e-10 tolerance."""
+    g = golden("slp1000_xi19")
     ps, f = g["psrc"], g["f"]
     ds = direct.slp_real_ds(ps[0], ps[1], ps[0], ps[1], f[0], f[1], 1.0, 1.0, g["xi"]) + \
         direct.slp_kspace_ds(ps[0], ps[1], ps[0], ps[1], f[0], f[1], 1.0, 1.0, g["xi"])
