@@ -68,8 +68,8 @@ UNIT = "evals/s"
 C_IN, C_OUT = 5, 4
 SPREAD_FLOP_PER_SOURCE = (P + 1) ** 2 * (1 + 2 * C_IN)
 GATHER_FLOP_PER_TARGET = (P + 1) ** 2 * (1 + 2 * C_OUT)
-DRAM_BYTES = {"spread": 2.878e9, "gather": 0.280e9, "real": 0.364e9}
-REAL_WARP_INST_PER_PAIR = 22.3     # ncu smsp__inst_executed / SLP+DLP pair evaluations
+DRAM_BYTES = {"spread": 2.832e9, "gather": 0.280e9, "real": 0.243e9}
+REAL_WARP_INST_PER_PAIR = 46.3     # ncu smsp__inst_executed / SLP+DLP pair evaluations
 
 
 def workload(N):

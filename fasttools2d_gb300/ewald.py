@@ -110,9 +110,13 @@ def _xi_dlp(Q, Lx, Ly, rc, tol):
     return _newton_limited(g, dg, 1 / rc, tol)
 
 
-def _kinf_dlp(Q, L1, L2, xi, tol):
-    # MATLAB parses sqrt(k*8*pi*Q*max(Lx,Ly)/Lx^3*Ly^3) as ((...)/Lx^3)*Ly^3.
-    c = math.sqrt(8 * math.pi * Q * max(L1, L2) / L1 ** 3 * L2 ** 3)
+def _kinf_dlp(Q, L1, L2, xi, tol, compat=True):
+    # MATLAB parses sqrt(k*8*pi*Q*max(Lx,Ly)/Lx^3*Ly^3) as ((...)/Lx^3)*Ly^3;
+    # compat=False uses the estimate's intended 1/(Lx^3 Ly^3).
+    if compat:
+        c = math.sqrt(8 * math.pi * Q * max(L1, L2) / L1 ** 3 * L2 ** 3)
+    else:
+        c = math.sqrt(8 * math.pi * Q * max(L1, L2) / (L1 ** 3 * L2 ** 3))
     s = 4 * xi * xi
     g = lambda k: c * math.sqrt(k) * math.exp(-k * k / s) - tol
     dg = lambda k: c * math.exp(-k * k / s) * (0.5 / math.sqrt(k) - 2 * k ** 1.5 / s)
@@ -121,8 +125,14 @@ def _kinf_dlp(Q, L1, L2, xi, tol):
 
 
 def select_params(kind: str, nsrc: int, ntar: int, fsq_sum: float, Lx: float, Ly: float,
-                  P: int = 24, Nb=None, tol: float = 1e-16) -> EwaldParams:
-    """Ewald parameters as the MATLAB drivers choose them; fsq_sum = sum(f.^2)."""
+                  P: int = 24, Nb=None, tol: float = 1e-16, compat: bool = True) -> EwaldParams:
+    """Ewald parameters as the MATLAB drivers choose them; fsq_sum = sum(f.^2).
+
+    compat=True (the default) reproduces the drivers' own arithmetic, so the
+    same inputs give the reference's xi, nside and M: the SLP k_inf estimate
+    receives (Lx, Lx) (StokesSLP_ewald_2p.m:96) and the DLP one keeps MATLAB's
+    parse of /Lx^3*Ly^3 (StokesDLP_ewald_2p.m:177).  compat=False passes
+    (Lx, Ly) and divides by Lx^3 Ly^3, as the estimates are written."""
     npts = nsrc + ntar
     if Nb is None:
         Nb = min(P * _round_half_away(math.log2(npts)), npts / 4)
@@ -131,12 +141,13 @@ def select_params(kind: str, nsrc: int, ntar: int, fsq_sum: float, Lx: float, Ly
     a = math.ceil(math.sqrt(npts / (Nb * A * B)))
     nside_x, nside_y = a * A, a * B
     rc = Lx / nside_x
+    L2 = Lx if compat else Ly
     if kind == "slp":
         xi = _xi_slp(Q, Lx, Ly, rc, tol)
-        kinf = _kinf_slp(Q, Lx, Lx, xi, tol)
+        kinf = _kinf_slp(Q, Lx, L2, xi, tol)
     elif kind == "dlp":
         xi = _xi_dlp(Q, Lx, Ly, rc, tol)
-        kinf = _kinf_dlp(Q, Lx, Lx, xi, tol)
+        kinf = _kinf_dlp(Q, Lx, L2, xi, tol, compat)
     else:
         raise ValueError("kind must be 'slp' or 'dlp'")
     M = min(2 * kinf, 10000)

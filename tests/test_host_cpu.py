@@ -84,3 +84,16 @@ def test_params_meet_estimated_tolerance():
     Q = 2e4 + 1
     est = np.sqrt(Q * np.pi / (4 * prm.xi)) * np.exp(-(prm.xi * rc) ** 2)
     assert 0 < est <= 2e-10
+
+
+def test_select_params_compat_switch():
+    """compat=True keeps the drivers' arithmetic; compat=False the estimates as
+    written.  They coincide for a unit square and differ for Lx != Ly."""
+    from fasttools2d_gb300.ewald import select_params
+    a = select_params("dlp", 4000, 4000, 3e3, 1.0, 1.0, tol=1e-10, compat=True)
+    b = select_params("dlp", 4000, 4000, 3e3, 1.0, 1.0, tol=1e-10, compat=False)
+    assert (a.xi, a.Mx, a.My) == (b.xi, b.Mx, b.My)
+    for kind, Ly in (("slp", 2.0), ("dlp", 8.0)):
+        c = select_params(kind, 4000, 4000, 3e3, 1.0, Ly, tol=1e-10, compat=True)
+        d = select_params(kind, 4000, 4000, 3e3, 1.0, Ly, tol=1e-10, compat=False)
+        assert c.xi == d.xi and c.Mx > d.Mx
