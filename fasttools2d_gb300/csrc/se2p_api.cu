@@ -40,6 +40,7 @@ enum Slot {
     S_IN_W1, S_IN_W2, S_WCOEF, S_GR, S_GK, S_SBOXS, S_ZEROS,   // adjoint
     S_FTAB,                                     // cached per-mode filter factors
     S_GTAB, S_COEF_FF,                          // float-float real space
+    S_ZGRID,                                    // complex pairs of grids (1D-pass FFT)
     S_COUNT_SLOTS
 };
 
@@ -257,7 +258,9 @@ int finish_out(se2p_plan pl, const OutBuf &o)
     return SE2P_OK;
 }
 
-// dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32)
+// dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32) -- 2D, batch grids;
+// 4 = Z2Z along y (batch contiguous rows of My); 5 = Z2Z along x of one
+// Mx x (My/2+1) half spectrum (stride My/2+1, My/2+1 transforms).
 int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, cufftHandle *h)
 {
     auto key = std::make_tuple(Mx, My, batch, dir);
@@ -270,6 +273,23 @@ int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, c
     int n[2] = {Mx, My};
     const int real_dist = Mx * My, cplx_dist = Mx * (My / 2 + 1);
     cufftHandle p;
+    if (dir == 4) {
+        int ny = My;
+        CKF(cufftPlanMany(&p, 1, &ny, nullptr, 1, My, nullptr, 1, My, CUFFT_Z2Z, batch));
+        CKF(cufftSetStream(p, st));
+        pl->ffts[key] = p;
+        *h = p;
+        return SE2P_OK;
+    }
+    if (dir == 5) {
+        int nx = Mx, emb = Mx;
+        const int H1 = My / 2 + 1;
+        CKF(cufftPlanMany(&p, 1, &nx, &emb, H1, 1, &emb, H1, 1, CUFFT_Z2Z, H1));
+        CKF(cufftSetStream(p, st));
+        pl->ffts[key] = p;
+        *h = p;
+        return SE2P_OK;
+    }
     const bool fwd = dir == 0 || dir == 2;
     const cufftType type = dir == 0 ? CUFFT_D2Z : dir == 1 ? CUFFT_Z2D : dir == 2 ? CUFFT_R2C : CUFFT_C2R;
     if (fwd)
@@ -736,11 +756,22 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             CK(launch_spread(sa, nc, ks, pl->launches));
         }
 
-        cufftHandle fwd, inv;
-        CKS(get_fft(pl, ks, Mx, My, nc, 0, &fwd));
+        // D2Z as 1D complex passes: pack pairs, C2C along y, split, C2C along x
+        const int ncg = (nc + 1) / 2, npo = (nout + 1) / 2;
+        cufftDoubleComplex *zg = nullptr;
+        CKS(ensure_t(pl, S_ZGRID, G * (size_t)std::max(ncg, npo), &zg));
+        double2 *zgd = reinterpret_cast<double2 *>(zg);
+        cufftHandle fy, fx;
+        CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
+        CKS(get_fft(pl, ks, Mx, My, 1, 5, &fx));
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
-            CKF(cufftExecD2Z(fwd, grid, spec));
+            CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
+            CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
+            CK(launch_split_half_spectra(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
+                                         pl->launches));
+            for (int c = 0; c < nc; c++)
+                CKF(cufftExecZ2Z(fx, spec + (size_t)c * H, spec + (size_t)c * H, CUFFT_FORWARD));
         }
 
         FilterArgs fa;
@@ -763,10 +794,18 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             CK(launch_filter(fa, ks, pl->launches));
         }
 
-        CKS(get_fft(pl, ks, Mx, My, nout, 1, &inv));
+        // Z2D as 1D complex passes: C2C along x, Hermitian join, C2C along y, unpack
+        cufftHandle iy;
+        CKS(get_fft(pl, ks, Mx, My, npo * Mx, 4, &iy));
+        CKS(get_fft(pl, ks, Mx, My, 1, 5, &fx));
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            CKF(cufftExecZ2D(inv, spec, grid));
+            for (int c = 0; c < nout; c++)
+                CKF(cufftExecZ2Z(fx, spec + (size_t)c * H, spec + (size_t)c * H, CUFFT_INVERSE));
+            CK(launch_join_half_spectra(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
+                                        pl->launches));
+            CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
+            CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches));
         }
 
         GatherArgs ga;

@@ -286,6 +286,17 @@ cudaError_t launch_src_coef_ff(int64_t n, const double *coef, int nc, bool slp, 
                                float2 *out, int ncf, cudaStream_t st, int64_t &launches);
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                         int64_t &launches, int form = kFormFP64);
+// 2D real FFT through 1D complex passes (se2p_kernels.cu): pack real grid
+// pairs as complex, split a y-transformed pair into half spectra, the inverse
+// Hermitian join, and the final real/imaginary unpack.
+cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,
+                                   cudaStream_t st, int64_t &launches);
+cudaError_t launch_split_half_spectra(const double2 *z, int nc, int Mx, int My, double2 *spec,
+                                      cudaStream_t st, int64_t &launches);
+cudaError_t launch_join_half_spectra(const double2 *spec, int nout, int Mx, int My, double2 *z,
+                                     cudaStream_t st, int64_t &launches);
+cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
+                                     cudaStream_t st, int64_t &launches);
 int sm_count();
 cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                             int64_t &launches, int form = kFormFP64);

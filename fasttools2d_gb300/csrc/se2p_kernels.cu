@@ -1395,6 +1395,90 @@ template __global__ void k_spread<3>(SpreadArgs);
 template __global__ void k_spread<5>(SpreadArgs);
 
 // ===========================================================================
+// 2D real FFT as two 1D complex passes (FP64 form).
+//
+// cuFFT's batched 1D R2C of length 2688 runs at half the rate of its C2C of
+// the same length, so the real grids are transformed as complex pairs:
+// z = a + i b for grids (2p, 2p+1), C2C along y (contiguous rows), split by
+// Hermitian symmetry into the half spectra A(ky) = (Z(ky) + conj Z(-ky))/2,
+// B(ky) = (Z(ky) - conj Z(-ky))/(2i) for ky = 0..My/2, then C2C along x on
+// each half spectrum -- the D2Z result.  The inverse mirrors it: C2C along x,
+// Hermitian extension in ky and packing z = A + i B, C2C along y, real and
+// imaginary parts -- the Z2D result (unnormalised, as cuFFT's).
+// ===========================================================================
+__global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64_t G,
+                                  double2 *__restrict__ z)
+{
+    const int ncg = (nc + 1) / 2;
+    const int64_t n = (int64_t)ncg * G;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / G);
+        const int64_t e = i - (int64_t)p * G;
+        const double re = grid[(int64_t)(2 * p) * G + e];
+        const double im = 2 * p + 1 < nc ? grid[(int64_t)(2 * p + 1) * G + e] : 0.0;
+        z[i] = make_double2(re, im);
+    }
+}
+
+__global__ void k_split_half_spectra(const double2 *__restrict__ z, int nc, int Mx, int My,
+                                     double2 *__restrict__ spec)
+{
+    const int H1 = My / 2 + 1;
+    const int64_t H = (int64_t)Mx * H1, G = (int64_t)Mx * My;
+    const int64_t n = (int64_t)nc * H;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i / H);
+        const int64_t r = i - (int64_t)c * H;
+        const int x = (int)(r / H1), ky = (int)(r - (int64_t)x * H1);
+        const double2 *row = z + (int64_t)(c >> 1) * G + (int64_t)x * My;
+        const double2 zk = row[ky], zm = row[ky == 0 ? 0 : My - ky];
+        spec[i] = (c & 1) ? make_double2(0.5 * (zk.y + zm.y), 0.5 * (zm.x - zk.x))
+                          : make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
+    }
+}
+
+__global__ void k_join_half_spectra(const double2 *__restrict__ spec, int nout, int Mx, int My,
+                                    double2 *__restrict__ z)
+{
+    const int H1 = My / 2 + 1;
+    const int64_t H = (int64_t)Mx * H1, G = (int64_t)Mx * My;
+    const int npair = (nout + 1) / 2;
+    const int64_t n = (int64_t)npair * G;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / G);
+        const int64_t r = i - (int64_t)p * G;
+        const int x = (int)(r / My), ky = (int)(r - (int64_t)x * My);
+        const bool hi = ky > My / 2;
+        const int64_t src = (int64_t)x * H1 + (hi ? My - ky : ky);
+        double2 a = spec[(int64_t)(2 * p) * H + src];
+        double2 b = 2 * p + 1 < nout ? spec[(int64_t)(2 * p + 1) * H + src] : make_double2(0.0, 0.0);
+        if (hi) {
+            a.y = -a.y;
+            b.y = -b.y;
+        }
+        z[i] = make_double2(a.x - b.y, a.y + b.x);
+    }
+}
+
+__global__ void k_unpack_real_pairs(const double2 *__restrict__ z, int nout, int64_t G,
+                                    double *__restrict__ grid)
+{
+    const int npair = (nout + 1) / 2;
+    const int64_t n = (int64_t)npair * G;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / G);
+        const int64_t e = i - (int64_t)p * G;
+        const double2 v = z[i];
+        grid[(int64_t)(2 * p) * G + e] = v.x;
+        if (2 * p + 1 < nout) grid[(int64_t)(2 * p + 1) * G + e] = v.y;
+    }
+}
+
+// ===========================================================================
 // k-space filter on the half spectrum (R2C layout Mx x (My/2+1)).
 //
 // The reference transforms real grids with a full complex fft2, applies the
@@ -2188,6 +2272,51 @@ cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, co
                                                          g_pos, g_fs, g_fd, g_n);
         launches++;
     }
+    return cudaGetLastError();
+}
+
+}  // namespace se2p
+
+namespace se2p {
+
+static unsigned stream_grid(int64_t n)
+{
+    const int64_t want = (n + 255) / 256, cap = (int64_t)sm_count() * 16;
+    return (unsigned)(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,
+                                   cudaStream_t st, int64_t &launches)
+{
+    k_pack_real_pairs<<<stream_grid((int64_t)((nc + 1) / 2) * G), 256, 0, st>>>(grid, nc, G, z);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_half_spectra(const double2 *z, int nc, int Mx, int My, double2 *spec,
+                                      cudaStream_t st, int64_t &launches)
+{
+    const int64_t n = (int64_t)nc * Mx * (My / 2 + 1);
+    k_split_half_spectra<<<stream_grid(n), 256, 0, st>>>(z, nc, Mx, My, spec);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_join_half_spectra(const double2 *spec, int nout, int Mx, int My, double2 *z,
+                                     cudaStream_t st, int64_t &launches)
+{
+    const int64_t n = (int64_t)((nout + 1) / 2) * Mx * My;
+    k_join_half_spectra<<<stream_grid(n), 256, 0, st>>>(spec, nout, Mx, My, z);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
+                                     cudaStream_t st, int64_t &launches)
+{
+    k_unpack_real_pairs<<<stream_grid((int64_t)((nout + 1) / 2) * G), 256, 0, st>>>(z, nout, G,
+                                                                                    grid);
+    launches++;
     return cudaGetLastError();
 }
 
