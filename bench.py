@@ -294,6 +294,45 @@ def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
 N5, XI5, RC5, M5, P5 = 2 ** 18, 430.0, 0.011, 1344, 24
 
 
+def multi_rhs_leg(plan, tens, N, ms_single, dev, nrhs=4):
+    """Many right-hand sides on the 1M-point geometry (se2p_geom_*): time to
+    build the geometry (sort, cell lists, real-space operator), and time per
+    right-hand side of one apply over nrhs densities, against the single-RHS
+    evaluation.  Every apply is checked against se2p_stokes_ewald on its
+    first right-hand side."""
+    import time
+    import torch
+    import fasttools2d_gb300 as ft
+    prm = ft.EwaldParams.derived(XI, int(math.floor(L / RC)), int(math.floor(L / RC)), M, M, P, L, L)
+    rng = torch.Generator(device=dev).manual_seed(SEED + 100)
+    F = torch.randn((nrhs, N, 2), dtype=torch.float64, device=dev, generator=rng)
+    G = torch.randn((nrhs, N, 2), dtype=torch.float64, device=dev, generator=rng)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    geo = ft.Geometry(tens[0], tens[1], prm, n=tens[4], plan=plan)
+    torch.cuda.synchronize(dev)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    us, ud = geo.apply(F, G)                       # warm-up (cuFFT plans, workspace)
+    best = 1e30
+    for _ in range(3):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        us, ud = geo.apply(F, G)
+        torch.cuda.synchronize(dev)
+        best = min(best, (time.perf_counter() - t0) * 1e3)
+    vs, vd = ft.stokes_ewald(tens[0], tens[1], F[0], G[0], tens[4], prm, plan=plan)
+    err = max(float((us[0] - vs).abs().max() / vs.abs().max()),
+              float((ud[0] - vd).abs().max() / vd.abs().max()))
+    out = {"workload": f"SE SLP+DLP, same 1M points and parameters, {nrhs} right-hand sides "
+                       "per apply (densities ~ N(0,1))",
+           "nrhs": nrhs, "geometry_build_ms": build_ms, "apply_ms_per_rhs": best / nrhs,
+           "single_rhs_ms": ms_single, "speedup_per_rhs": ms_single / (best / nrhs),
+           "geometry_bytes": geo.bytes, "pairs": geo.pairs,
+           "max_rel_diff_vs_single_rhs": err}
+    geo.close()
+    return out
+
+
 def adjoint_leg(plan, steps, timed, dev):
     """Adjoint workload: time of the forward and of forward + adjoint (gradients of
     J = sum_t w_slp.u_slp + w_dlp.u_dlp w.r.t. source positions, forces,
@@ -480,6 +519,7 @@ def gpu_arm(args, rank, world, local_rank):
     mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev) \
         if "fp32_grid" in legs else None
     adjoint = adjoint_leg(plan, args.steps, timed, dev) if "adjoint" in legs else None
+    multi = multi_rhs_leg(plan, tens, N, ms_per_step, dev) if "multi_rhs" in legs else None
 
     # ---- roofline of the dominant kernel ---------------------------------
     # Stage times come from CUDA events on each kernel's own stream, taken in
@@ -526,6 +566,7 @@ def gpu_arm(args, rank, world, local_rank):
         "config": config(N, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
         "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
         "clocks": clk.summary(), "fp32_grid": mixed, "adjoint": adjoint,
+        "multi_rhs": multi,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N)
@@ -542,8 +583,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="points (sources = targets count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--legs", default="fp32_grid,adjoint",
-                    help="extra legs after the headline workload: fp32_grid, adjoint, or none "
+    ap.add_argument("--legs", default="fp32_grid,adjoint,multi_rhs",
+                    help="extra legs after the headline workload: fp32_grid, adjoint, multi_rhs, "
+                         "or none "
                          "(a profiling run of the headline workload alone uses none)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -27,6 +27,8 @@ EXPORTS = (
     "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
     "se2p_plan_count_pairs", "se2p_slp_real_noalloc", "se2p_plan_set_precision",
     "se2p_plan_set_overlap", "se2p_stokes_ewald_adjoint",
+    "se2p_geom_create", "se2p_geom_apply", "se2p_geom_bytes", "se2p_geom_pairs",
+    "se2p_geom_destroy",
 )
 PRECISION_FP64, PRECISION_FP32_GRID, PRECISION_FP64_NATIVE = 0, 1, 2
 _PRECISIONS = {"fp64": PRECISION_FP64, "fp32_grid": PRECISION_FP32_GRID,
@@ -93,6 +95,13 @@ def load(path: str = LIB_PATH):
         L.se2p_stokes_ewald.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp]
         L.se2p_stokes_ewald_adjoint.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, _dp, _dp, _dp, _dp,
                                                 _dp, _dp, _dp, _dp]
+        L.se2p_geom_create.argtypes = [P, PP, _dp, i64, _dp, i64, _dp, i32, ctypes.POINTER(P)]
+        L.se2p_geom_apply.argtypes = [P, i32, _dp, _dp, _dp, _dp]
+        L.se2p_geom_bytes.argtypes = [P]
+        L.se2p_geom_bytes.restype = i64
+        L.se2p_geom_pairs.argtypes = [P]
+        L.se2p_geom_pairs.restype = i64
+        L.se2p_geom_destroy.argtypes = [P]
         for name in EXPORTS:
             if name not in ("se2p_version",):
                 getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int

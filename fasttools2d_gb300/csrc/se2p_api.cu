@@ -41,6 +41,8 @@ enum Slot {
     S_FTAB,                                     // cached per-mode filter factors
     S_GTAB, S_COEF_FF,                          // float-float real space
     S_ZGRID,                                    // complex pairs of grids (1D-pass FFT)
+    S_GCOUNT, S_GTGT, S_GMETA,                  // geometry build scratch
+    S_GCOEF, S_GCOEFF, S_GUR0, S_GUR1,          // geometry apply scratch
     S_COUNT_SLOTS
 };
 
@@ -1416,6 +1418,305 @@ int se2p_stokes_ewald(se2p_plan pl, const se2p_params *prm, const double *psrc, 
     io.ns = ns; io.nt = nt;
     io.u_slp = u_slp; io.u_dlp = u_dlp; io.mode_slp = 3; io.mode_dlp = 4;
     return run(pl, J, io);
+}
+
+// --------------------------------------------------------------------------
+// Reusable geometry: sorted points, cell lists and the real-space operator of
+// one point set, applied to many right-hand sides (se2p_geom.cu).
+// --------------------------------------------------------------------------
+struct se2p_geom_st {
+    se2p_plan pl = nullptr;
+    se2p_params prm{};
+    bool slp = false, dlp = false;
+    int64_t ns = 0, nt = 0, nnz = 0;
+    std::vector<void *> owned;
+    size_t bytes = 0;
+    double2 *ps = nullptr, *pt = nullptr, *nr = nullptr;   // caller's arrays, original order
+    double2 *sp = nullptr, *tp = nullptr;                  // sorted, wrapped
+    float2 *spf = nullptr, *tpf = nullptr;
+    int *sperm = nullptr, *tperm = nullptr, *tboxs = nullptr, *sstart = nullptr;
+    int *rowptr = nullptr, *src = nullptr;
+    float2 *cf = nullptr;
+    // apply scratch (grown on demand): staged RHS and outputs
+    double2 *fin = nullptr, *din = nullptr, *uout = nullptr;
+    size_t fin_n = 0, din_n = 0, uout_n = 0;
+};
+
+extern "C++" {
+template <class T>
+int geom_alloc(se2p_geom g, size_t count, T **out)
+{
+    void *p = nullptr;
+    const size_t bytes = (count ? count : 1) * sizeof(T);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(g->pl, SE2P_ERR_ALLOC, "geometry: cudaMalloc(%zu bytes) failed", bytes);
+    }
+    g->owned.push_back(p);
+    g->bytes += bytes;
+    *out = static_cast<T *>(p);
+    return SE2P_OK;
+}
+}  // extern "C++"
+
+static void geom_free(se2p_geom g)
+{
+    for (void *p : g->owned) cudaFree(p);
+    g->owned.clear();
+    g->bytes = 0;
+}
+
+// Grows one apply buffer (freeing the old one).
+static int geom_grow(se2p_geom g, double2 **buf, size_t *have, size_t want)
+{
+    se2p_plan pl = g->pl;
+    if (*have >= want && *buf) return SE2P_OK;
+    if (*buf) {
+        CK(cudaStreamSynchronize(pl->stream));
+        for (auto it = g->owned.begin(); it != g->owned.end(); ++it)
+            if (*it == *buf) {
+                cudaFree(*it);
+                g->owned.erase(it);
+                g->bytes -= *have * sizeof(double2);
+                break;
+            }
+        *buf = nullptr;
+        *have = 0;
+    }
+    CKS(geom_alloc(g, want, buf));
+    *have = want;
+    return SE2P_OK;
+}
+
+static int geom_build(se2p_geom g, const double *psrc, const double *ptar, const double *n)
+{
+    se2p_plan pl = g->pl;
+    cudaStream_t st = pl->stream;
+    const se2p_params &p = g->prm;
+    const int64_t ns = g->ns, nt = g->nt;
+    const int nx = p.nside_x, ny = p.nside_y, nbox = nx * ny;
+    const size_t nsz = (size_t)(ns > 0 ? ns : 1), ntz = (size_t)(nt > 0 ? nt : 1);
+    CKS(geom_alloc(g, nsz, &g->ps));
+    CKS(geom_alloc(g, ntz, &g->pt));
+    if (ns > 0) CK(cudaMemcpyAsync(g->ps, psrc, 16 * (size_t)ns, cudaMemcpyDefault, st));
+    if (nt > 0) CK(cudaMemcpyAsync(g->pt, ptar, 16 * (size_t)nt, cudaMemcpyDefault, st));
+    if (g->dlp) {
+        CKS(geom_alloc(g, nsz, &g->nr));
+        if (ns > 0) CK(cudaMemcpyAsync(g->nr, n, 16 * (size_t)ns, cudaMemcpyDefault, st));
+    }
+    CKS(geom_alloc(g, nsz, &g->sp));
+    CKS(geom_alloc(g, ntz, &g->tp));
+    CKS(geom_alloc(g, nsz, &g->spf));
+    CKS(geom_alloc(g, ntz, &g->tpf));
+    CKS(geom_alloc(g, nsz, &g->sperm));
+    CKS(geom_alloc(g, ntz, &g->tperm));
+    CKS(geom_alloc(g, ntz, &g->tboxs));
+    CKS(geom_alloc(g, (size_t)nbox + 1, &g->sstart));
+    CKS(geom_alloc(g, ntz + 1, &g->rowptr));
+    // wrap, then sort into the real-space boxes
+    double2 *ws = nullptr, *wt = nullptr;
+    int *sbox, *srank, *tbox, *trank, *count, *tstart;
+    CKS(ensure_t(pl, S_WPS, nsz, &ws));
+    CKS(ensure_t(pl, S_WPT, ntz, &wt));
+    CKS(ensure_t(pl, S_SBOX, nsz, &sbox));
+    CKS(ensure_t(pl, S_SRANK, nsz, &srank));
+    CKS(ensure_t(pl, S_TBOX, ntz, &tbox));
+    CKS(ensure_t(pl, S_TRANK, ntz, &trank));
+    CKS(ensure_t(pl, S_COUNT, (size_t)nbox, &count));
+    CKS(ensure_t(pl, S_TSTART, (size_t)nbox + 1, &tstart));
+    if (ns > 0) CK(launch_wrap(ns, g->ps, p.Lx, p.Ly, ws, st, pl->launches));
+    if (nt > 0) CK(launch_wrap(nt, g->pt, p.Lx, p.Ly, wt, st, pl->launches));
+    BinArgs bs{ws, ns, p.Lx, p.Ly, nx, ny, sbox, srank, count};
+    CK(launch_bin(bs, g->sstart, nbox, g->sperm, nullptr, g->sp, g->spf, st, pl->launches));
+    BinArgs bt{wt, nt, p.Lx, p.Ly, nx, ny, tbox, trank, count};
+    CK(launch_bin(bt, tstart, nbox, g->tperm, g->tboxs, g->tp, g->tpf, st, pl->launches));
+
+    RealArgs ra{};
+    ra.sp = g->sp;
+    ra.spf = g->spf;
+    ra.sstart = g->sstart;
+    ra.tp = g->tp;
+    ra.tpf = g->tpf;
+    ra.tbox = g->tboxs;
+    ra.ntar = nt;
+    ra.nx = nx;
+    ra.ny = ny;
+    ra.Lx = p.Lx;
+    ra.Ly = p.Ly;
+    ra.xi = p.xi;
+    ra.xi2 = p.xi * p.xi;
+    ra.cut2 = p.Lx * p.Ly / nx / ny;                  // mex_stokes_slp_real.cpp:127
+    ra.cut2f = (float)ra.cut2;
+    ra.xi2f = (float)(p.xi * p.xi);
+    ra.inv_xi2 = 1.0 / (p.xi * p.xi);
+    ra.pf = 2.0 * p.xi * p.xi;
+    ra.zxm = (p.Lx * (double)(-nx)) / nx;
+    ra.zxp = (p.Lx * (double)nx) / nx;
+    ra.zym = (p.Ly * (double)(-ny)) / ny;
+    ra.zyp = (p.Ly * (double)ny) / ny;
+    ra.self_c = -1.288607832450766155 - std::log(p.xi);  // mex_stokes_slp_real.cpp:124
+    CKS(gtab_device(pl, st, &ra.gtab));
+
+    int *rowcnt = nullptr;
+    CKS(ensure_t(pl, S_GCOUNT, ntz, &rowcnt));
+    CK(launch_geom_rows(ra, g->slp, g->dlp, false, rowcnt, nullptr, nullptr, nullptr, nullptr,
+                        st, pl->launches));
+    if (nt > 0) CK(launch_scan(rowcnt, (int)nt, g->rowptr, st, pl->launches));
+    else CK(cudaMemsetAsync(g->rowptr, 0, sizeof(int), st));
+    int nnz = 0;
+    CK(cudaMemcpyAsync(&nnz, g->rowptr + nt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (nnz < 0) return fail(pl, SE2P_ERR_UNSUPPORTED, "geometry: more than 2^31-1 pairs");
+    g->nnz = nnz;
+    const size_t nz = (size_t)(nnz > 0 ? nnz : 1);
+    CKS(geom_alloc(g, nz, &g->src));
+    CKS(geom_alloc(g, 7 * nz, &g->cf));
+    int *tgt = nullptr;
+    unsigned char *meta = nullptr;
+    CKS(ensure_t(pl, S_GTGT, nz, &tgt));
+    CKS(ensure_t(pl, S_GMETA, nz, &meta));
+    CK(launch_geom_rows(ra, g->slp, g->dlp, true, nullptr, g->rowptr, g->src, tgt, meta, st,
+                        pl->launches));
+    CK(launch_geom_coef(ra, g->slp, g->dlp, nnz, g->src, tgt, meta, g->cf, st, pl->launches));
+    CK(cudaStreamSynchronize(st));
+    return SE2P_OK;
+}
+
+int se2p_geom_create(se2p_plan pl, const se2p_params *prm, const double *psrc, int64_t ns,
+                     const double *ptar, int64_t nt, const double *n, int kinds, se2p_geom *geom)
+{
+    if (!pl || !geom) return SE2P_ERR_ARG;
+    *geom = nullptr;
+    CKS(check_params(pl, prm));
+    CKS(check_common(pl, psrc, ns, ptar, nt, prm->xi, prm->Lx, prm->Ly, ptar));
+    if (kinds < 1 || kinds > 3) return fail(pl, SE2P_ERR_ARG, "kinds must be 1 (SLP), 2 (DLP) or 3");
+    if ((kinds & 2) && ns > 0 && !n) return fail(pl, SE2P_ERR_ARG, "null n");
+    DeviceGuard guard(pl->device);
+    se2p_geom g = new se2p_geom_st;
+    g->pl = pl;
+    g->prm = *prm;
+    g->slp = (kinds & 1) != 0;
+    g->dlp = (kinds & 2) != 0;
+    g->ns = ns;
+    g->nt = nt;
+    const int rc = geom_build(g, psrc, ptar, n);
+    if (rc != SE2P_OK) {
+        cudaStreamSynchronize(pl->stream);
+        geom_free(g);
+        delete g;
+        return rc;
+    }
+    *geom = g;
+    return SE2P_OK;
+}
+
+int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_dlp,
+                    double *u_slp, double *u_dlp)
+{
+    if (!g) return SE2P_ERR_ARG;
+    se2p_plan pl = g->pl;
+    DeviceGuard guard(pl->device);
+    cudaStream_t st = pl->stream;
+    const int64_t ns = g->ns, nt = g->nt;
+    if (nrhs < 0) return fail(pl, SE2P_ERR_ARG, "negative nrhs");
+    if (nrhs == 0 || nt == 0) return SE2P_OK;
+    if (g->slp && ((ns > 0 && !f_slp) || !u_slp)) return fail(pl, SE2P_ERR_ARG, "null f_slp / u_slp");
+    if (g->dlp && ((ns > 0 && !f_dlp) || !u_dlp)) return fail(pl, SE2P_ERR_ARG, "null f_dlp / u_dlp");
+    const size_t nsz = (size_t)(ns > 0 ? ns : 1);
+    // RHS in device memory, original order (one copy each, whatever their origin)
+    if (g->slp) {
+        CKS(geom_grow(g, &g->fin, &g->fin_n, (size_t)nrhs * nsz));
+        if (ns > 0)
+            CK(cudaMemcpyAsync(g->fin, f_slp, 16 * (size_t)ns * nrhs, cudaMemcpyDefault, st));
+    }
+    if (g->dlp) {
+        CKS(geom_grow(g, &g->din, &g->din_n, (size_t)nrhs * nsz));
+        if (ns > 0)
+            CK(cudaMemcpyAsync(g->din, f_dlp, 16 * (size_t)ns * nrhs, cudaMemcpyDefault, st));
+    }
+    const int nk = (g->slp ? 1 : 0) + (g->dlp ? 1 : 0);
+    CKS(geom_grow(g, &g->uout, &g->uout_n, (size_t)nk * nrhs * nt));
+    double2 *uo_slp = g->uout, *uo_dlp = g->uout + (g->slp ? (size_t)nrhs * nt : 0);
+
+    const int nc = (g->slp ? 2 : 0) + (g->dlp ? 3 : 0);
+    const int ncf = (g->slp ? 2 : 0) + (g->dlp ? 5 : 0);
+    const int doff_ff = g->slp ? 2 : 0;
+    constexpr int kBatch = 4;
+    double *coef = nullptr;
+    float2 *cff = nullptr;
+    double2 *ur0 = nullptr, *ur1 = nullptr;
+    CKS(ensure_t(pl, S_GCOEF, (size_t)kBatch * nc * nsz, &coef));
+    CKS(ensure_t(pl, S_GCOEFF, (size_t)kBatch * ncf * nsz, &cff));
+    if (g->slp) CKS(ensure_t(pl, S_GUR0, (size_t)kBatch * nt, &ur0));
+    if (g->dlp) CKS(ensure_t(pl, S_GUR1, (size_t)kBatch * nt, &ur1));
+    for (int r0 = 0; r0 < nrhs; r0 += kBatch) {
+        const int nb = std::min(kBatch, nrhs - r0);
+        // real space: float-float coefficients of each RHS, then the sparse product
+        for (int r = 0; r < nb; r++) {
+            const double2 *fs = g->slp ? g->fin + (size_t)(r0 + r) * ns : nullptr;
+            const double2 *fd = g->dlp ? g->din + (size_t)(r0 + r) * ns : nullptr;
+            double *cr = coef + (size_t)r * nc * nsz;
+            CK(launch_src_coef(ns, g->sperm, fs, fd, g->nr, cr, nc, st, pl->launches));
+            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf * nsz, ncf,
+                                  st, pl->launches));
+        }
+        {
+            StageTimer tm(pl, T_REAL);
+            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nnz, g->rowptr, g->src, g->cf, cff, ncf,
+                                 doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+                                 (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, st, pl->launches));
+        }
+        // k space (and the DLP zero mode and sign) per RHS through the drivers'
+        // path, then the real-space part added in the caller's order
+        for (int r = 0; r < nb; r++) {
+            const int rr = r0 + r;
+            Job J;
+            job_from_params(J, &g->prm);
+            J.real = false;
+            J.slp = g->slp;
+            J.dlp = g->dlp;
+            J.zero_mode = g->dlp;
+            Io io;
+            io.psrc = reinterpret_cast<const double *>(g->ps);
+            io.ptar = reinterpret_cast<const double *>(g->pt);
+            io.f_slp = g->slp ? reinterpret_cast<const double *>(g->fin + (size_t)rr * ns) : nullptr;
+            io.f_dlp = g->dlp ? reinterpret_cast<const double *>(g->din + (size_t)rr * ns) : nullptr;
+            io.nrm = g->dlp ? reinterpret_cast<const double *>(g->nr) : nullptr;
+            io.ns = ns;
+            io.nt = nt;
+            io.u_slp = g->slp ? reinterpret_cast<double *>(uo_slp + (size_t)rr * nt) : nullptr;
+            io.u_dlp = g->dlp ? reinterpret_cast<double *>(uo_dlp + (size_t)rr * nt) : nullptr;
+            io.mode_slp = 3;
+            io.mode_dlp = 4;
+            CKS(run(pl, J, io));
+            if (g->slp)
+                CK(launch_geom_add(nt, g->tperm, ur0 + (size_t)r * nt, false, uo_slp + (size_t)rr * nt,
+                                   st, pl->launches));
+            if (g->dlp)
+                CK(launch_geom_add(nt, g->tperm, ur1 + (size_t)r * nt, true, uo_dlp + (size_t)rr * nt,
+                                   st, pl->launches));
+        }
+    }
+    if (g->slp)
+        CK(cudaMemcpyAsync(u_slp, uo_slp, 16 * (size_t)nt * nrhs, cudaMemcpyDefault, st));
+    if (g->dlp)
+        CK(cudaMemcpyAsync(u_dlp, uo_dlp, 16 * (size_t)nt * nrhs, cudaMemcpyDefault, st));
+    CK(cudaStreamSynchronize(st));
+    return SE2P_OK;
+}
+
+int64_t se2p_geom_bytes(se2p_geom g) { return g ? (int64_t)g->bytes : 0; }
+
+int64_t se2p_geom_pairs(se2p_geom g) { return g ? g->nnz : 0; }
+
+int se2p_geom_destroy(se2p_geom g)
+{
+    if (!g) return SE2P_OK;
+    DeviceGuard guard(g->pl->device);
+    cudaStreamSynchronize(g->pl->stream);
+    geom_free(g);
+    delete g;
+    return SE2P_OK;
 }
 
 int se2p_stokes_ewald_adjoint(se2p_plan pl, const se2p_params *prm, const double *psrc,

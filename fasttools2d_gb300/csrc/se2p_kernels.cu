@@ -9,7 +9,6 @@
 // work, the spread walks a flattened (P+1)^2 stencil, and the gather gives
 // each lane its own target.  Index, compare and shuffle work is nearly free
 // next to the FP64 pipe.
-#include "se2p_ff.cuh"
 #include "se2p_internal.cuh"
 
 namespace se2p {
@@ -196,72 +195,8 @@ constexpr int kRing = 32;     // targets in flight per warp
 __constant__ int c_nb_dx[9] = {0, -1, -1, -1, 0, 0, 1, 1, 1};
 __constant__ int c_nb_dy[9] = {0, -1, 0, 1, -1, 1, -1, 0, 1};
 
-// 2^(-j/64), j = 0..63, correctly rounded.
-__constant__ double c_exp_tab[64] = {
-    0x1.0000000000000p+0,
-    0x1.fa7c1819e90d8p-1,
-    0x1.f50765b6e4540p-1,
-    0x1.efa1bee615a27p-1,
-    0x1.ea4afa2a490dap-1,
-    0x1.e502ee78b3ff6p-1,
-    0x1.dfc97337b9b5fp-1,
-    0x1.da9e603db3285p-1,
-    0x1.d5818dcfba487p-1,
-    0x1.d072d4a07897cp-1,
-    0x1.cb720dcef9069p-1,
-    0x1.c67f12e57d14bp-1,
-    0x1.c199bdd85529cp-1,
-    0x1.bcc1e904bc1d2p-1,
-    0x1.b7f76f2fb5e47p-1,
-    0x1.b33a2b84f15fbp-1,
-    0x1.ae89f995ad3adp-1,
-    0x1.a9e6b5579fdbfp-1,
-    0x1.a5503b23e255dp-1,
-    0x1.a0c667b5de565p-1,
-    0x1.9c49182a3f090p-1,
-    0x1.97d829fde4e50p-1,
-    0x1.93737b0cdc5e5p-1,
-    0x1.8f1ae99157736p-1,
-    0x1.8ace5422aa0dbp-1,
-    0x1.868d99b4492edp-1,
-    0x1.82589994cce13p-1,
-    0x1.7e2f336cf4e62p-1,
-    0x1.7a11473eb0187p-1,
-    0x1.75feb564267c9p-1,
-    0x1.71f75e8ec5f74p-1,
-    0x1.6dfb23c651a2fp-1,
-    0x1.6a09e667f3bcdp-1,
-    0x1.6623882552225p-1,
-    0x1.6247eb03a5585p-1,
-    0x1.5e76f15ad2148p-1,
-    0x1.5ab07dd485429p-1,
-    0x1.56f4736b527dap-1,
-    0x1.5342b569d4f82p-1,
-    0x1.4f9b2769d2ca7p-1,
-    0x1.4bfdad5362a27p-1,
-    0x1.486a2b5c13cd0p-1,
-    0x1.44e086061892dp-1,
-    0x1.4160a21f72e2ap-1,
-    0x1.3dea64c123422p-1,
-    0x1.3a7db34e59ff7p-1,
-    0x1.371a7373aa9cbp-1,
-    0x1.33c08b26416ffp-1,
-    0x1.306fe0a31b715p-1,
-    0x1.2d285a6e4030bp-1,
-    0x1.29e9df51fdee1p-1,
-    0x1.26b4565e27cddp-1,
-    0x1.2387a6e756238p-1,
-    0x1.2063b88628cd6p-1,
-    0x1.1d4873168b9aap-1,
-    0x1.1a35beb6fcb75p-1,
-    0x1.172b83c7d517bp-1,
-    0x1.1429aaea92de0p-1,
-    0x1.11301d0125b51p-1,
-    0x1.0e3ec32d3d1a2p-1,
-    0x1.0b5586cf9890fp-1,
-    0x1.0874518759bc8p-1,
-    0x1.059b0d3158574p-1,
-    0x1.02c9a3e778061p-1};
+// 2^(-j/64), j = 0..63, correctly rounded (table in se2p_internal.cuh).
+__constant__ double c_exp_tab[64] = SE2P_EXP2_TAB64;
 
 // The three E1 Pade sets (layout in se2p_internal.cuh).
 __constant__ double c_e1[3][22] = SE2P_E1_PADE;
@@ -516,32 +451,6 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
         d1 = fmaf(ex, fmaf(fq, x1, pf * A1), d1);
         d2 = fmaf(ex, fmaf(fq, x2, pf * A2), d2);
     }
-}
-
-// g(x) = exp(x) E1(x) in the reference's Pade form (mid set below 16, far
-// set from 16 on), from the piecewise fit gtab, for 1 < x < 64.  The piece
-// follows from the head's exponent and top six mantissa bits; x = 16 with a
-// negative tail belongs to the mid set's last piece.
-__device__ __forceinline__ float2 ff_g_e1(float2 x, const float4 *__restrict__ gtab)
-{
-    const unsigned xb = __float_as_uint(x.x);
-    int oct = (int)(xb >> 23) - 127;
-    int m = (int)((xb >> 17) & 63u);
-    if (x.x == 16.0f && x.y < 0.0f) {
-        oct = 3;
-        m = 63;
-    }
-    const float c = __uint_as_float(((unsigned)(oct + 127) << 23) | ((unsigned)m << 17) | (1u << 16));
-    float dh, dl;
-    fast_two_sum(x.x - c, x.y, dh, dl);           // x.x - c is exact (same binade)
-    const float2 d = make_float2(dh, dl);
-    const float4 *cf = gtab + 3 * (oct * kGPiecesPerOctave + m);
-    const float4 A = __ldg(cf), B = __ldg(cf + 1), C = __ldg(cf + 2);
-    const float t = fmaf(fmaf(C.z, dh, C.y), dh, C.x);
-    float2 p = ff_add(make_float2(B.z, B.w), ff_mul_f(d, t));
-    p = ff_add(make_float2(B.x, B.y), ff_mul(p, d));
-    p = ff_add(make_float2(A.z, A.w), ff_mul(p, d));
-    return ff_add(make_float2(A.x, A.y), ff_mul(p, d));
 }
 
 // A pair in float-float (FP64 form, far pairs 1 < xi^2 r^2 < 64): the offset
@@ -2316,6 +2225,18 @@ cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, doub
 {
     k_unpack_real_pairs<<<stream_grid((int64_t)((nout + 1) / 2) * G), 256, 0, st>>>(z, nout, G,
                                                                                     grid);
+    launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace se2p
+
+namespace se2p {
+
+// Exclusive scan of n counts into start[0..n] (one block).
+cudaError_t launch_scan(const int *count, int n, int *start, cudaStream_t st, int64_t &launches)
+{
+    k_scan<<<1, 1024, 0, st>>>(count, n, start);
     launches++;
     return cudaGetLastError();
 }

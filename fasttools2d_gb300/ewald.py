@@ -304,3 +304,105 @@ def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=
     u, ur, uk = dlp_ewald(np.vstack([xs, ys]), np.vstack([xt, yt]), f, np.vstack([n1, n2]), prm,
                           parts=True, plan=plan)
     return u[0], u[1], ur, uk, prm.xi
+
+
+class Geometry:
+    """One point set for many right-hand sides (se2p_geom_*).
+
+    Sorts the points, builds the cell lists and stores the real-space
+    operator once; :meth:`apply` then evaluates any number of densities, each
+    exactly as :func:`stokes_ewald` (or :func:`slp_ewald` / :func:`dlp_ewald`
+    for one kind) would.  ``kinds`` is "slp", "dlp" or "both"; normals ``n``
+    belong to the geometry (DLP).  Arrays are MATLAB-shaped 2xN numpy arrays
+    or (N, 2) CUDA tensors, as elsewhere in this package.
+    """
+
+    _KINDS = {"slp": 1, "dlp": 2, "both": 3}
+
+    def __init__(self, psrc, ptar, prm: EwaldParams, n=None, kinds: str = "both", plan=None):
+        self.plan = _plan(plan)
+        self.kinds = self._KINDS[kinds]
+        self.prm = prm
+        s, t, nn = _Arg(psrc, "psrc"), _Arg(ptar, "ptar"), _Arg(n, "n")
+        if self.kinds & 2:
+            _same_n(s, nn, "psrc and n must be the same size.")
+        self.ns, self.nt, self.torch = s.n, t.n, t.torch
+        self.handle = ctypes.c_void_p()
+        c = prm.as_c()
+        self.plan.check(self.plan.lib.se2p_geom_create(self.plan.handle, ctypes.byref(c), s.ptr,
+                                                       s.n, t.ptr, t.n, nn.ptr, self.kinds,
+                                                       ctypes.byref(self.handle)))
+
+    @property
+    def bytes(self) -> int:
+        return self.plan.lib.se2p_geom_bytes(self.handle)
+
+    @property
+    def pairs(self) -> int:
+        return self.plan.lib.se2p_geom_pairs(self.handle)
+
+    def _rhs(self, f, name):
+        """nrhs x 2 x N numpy (or nrhs x N x 2 CUDA tensor) -> (pointer, nrhs, keep)."""
+        if f is None:
+            return None, None, None
+        if _is_torch(f):
+            import torch
+            t = f.to(torch.float64).contiguous()
+            if t.dim() != 3 or t.shape[1] != self.ns or t.shape[2] != 2:
+                raise ValueError(f"{name} must be an (nrhs, nsrc, 2) CUDA tensor")
+            return t.data_ptr(), t.shape[0], t
+        x = np.asarray(f, dtype=np.float64)
+        if x.ndim == 2:
+            x = x[None]
+        if x.ndim != 3 or x.shape[1] != 2 or x.shape[2] != self.ns:
+            raise ValueError(f"{name} must be nrhs x 2 x nsrc")
+        buf = np.ascontiguousarray(np.transpose(x, (0, 2, 1)))
+        return buf.ctypes.data, x.shape[0], buf
+
+    def apply(self, f_slp=None, f_dlp=None):
+        """u for each right-hand side: (u_slp, u_dlp), each nrhs x 2 x ntar (or
+        nrhs x ntar x 2 tensors); the kind not in the geometry is None."""
+        ps, ns_, ks = self._rhs(f_slp if self.kinds & 1 else None, "f_slp")
+        pd, nd_, kd = self._rhs(f_dlp if self.kinds & 2 else None, "f_dlp")
+        nrhs = ns_ if ns_ is not None else nd_
+        if nrhs is None:
+            raise ValueError("no right-hand side given")
+        if ns_ is not None and nd_ is not None and ns_ != nd_:
+            raise ValueError("f_slp and f_dlp must hold the same number of right-hand sides")
+        use_torch = any(k is not None and not isinstance(k, np.ndarray) for k in (ks, kd))
+        outs = []
+        for on in (self.kinds & 1, self.kinds & 2):
+            if not on:
+                outs.append(None)
+            elif use_torch:
+                import torch
+                outs.append(torch.empty((nrhs, self.nt, 2), dtype=torch.float64,
+                                        device=f"cuda:{self.plan.device}"))
+            else:
+                outs.append(np.zeros((nrhs, self.nt, 2)))
+        ptr = lambda o: None if o is None else (o.data_ptr() if not isinstance(o, np.ndarray)
+                                                 else o.ctypes.data)
+        self.plan.check(self.plan.lib.se2p_geom_apply(self.handle, nrhs, ps, pd, ptr(outs[0]),
+                                                      ptr(outs[1])))
+        res = []
+        for o in outs:
+            if o is None or not isinstance(o, np.ndarray):
+                res.append(o)
+            else:
+                res.append(np.transpose(o, (0, 2, 1)).copy())
+        return tuple(res)
+
+    def close(self):
+        if self.handle:
+            self.plan.lib.se2p_geom_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")

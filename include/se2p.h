@@ -180,6 +180,34 @@ int se2p_stokes_ewald_adjoint(se2p_plan plan, const se2p_params *prm, const doub
                               const double *w_slp, const double *w_dlp, double *g_psrc,
                               double *g_fslp, double *g_fdlp, double *g_n);
 
+/* ---- reusable geometry: many right-hand sides on one point set ---------------
+ * No reference counterpart.  Boundary-integral solvers apply the same SE
+ * operator to a new density every GMRES iteration.  se2p_geom_create sorts
+ * the sources and targets once, builds the cell lists and precomputes the
+ * real-space operator for prm: per target, every accepted (source, pair) with
+ * its SLP 2x2 block (h - g x2^2, g x1 x2, h - g x1^2) and DLP 2x3 block --
+ * float-float for far pairs, FP64 for near pairs and the self term (60 bytes
+ * per pair; se2p_geom_bytes reports the total, about 6.6 GB at 2^20 + 2^20
+ * uniform points with nside = 178).  kinds
+ * = 1 (SLP), 2 (DLP, normals n fixed with the geometry) or 3 (both).
+ * se2p_geom_apply evaluates nrhs right-hand sides -- f_slp and f_dlp are nrhs
+ * consecutive 2 x nsrc arrays, u_slp and u_dlp nrhs consecutive 2 x ntar
+ * arrays, host or device -- each as se2p_stokes_ewald (or se2p_slp_ewald /
+ * se2p_dlp_ewald for one kind) would: the real space by the stored operator
+ * (several RHS per pass over it), the k space and the DLP k=0 term per RHS at
+ * the plan's precision.  Results agree with the single-RHS entry points to
+ * ~1e-13.  The geometry uses its plan's stream and workspace: destroy it
+ * before the plan, and do not run it concurrently with other calls on the plan. */
+typedef struct se2p_geom_st *se2p_geom;
+int se2p_geom_create(se2p_plan plan, const se2p_params *prm, const double *psrc, int64_t nsrc,
+                     const double *ptar, int64_t ntar, const double *n, int kinds,
+                     se2p_geom *geom);
+int se2p_geom_apply(se2p_geom geom, int nrhs, const double *f_slp, const double *f_dlp,
+                    double *u_slp, double *u_dlp);
+int64_t se2p_geom_bytes(se2p_geom geom);
+int64_t se2p_geom_pairs(se2p_geom geom);
+int se2p_geom_destroy(se2p_geom geom);
+
 /* ---- allocation-free SLP real space ------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: a MEX function running inside MATLAB, where gpuArray's caching
