@@ -77,7 +77,7 @@ struct se2p_plan_st {
     bool overlap = true;             // real space concurrent with the k-space chain
     bool timing = false;
     bool count_pairs = false;
-    double ftab_key[6] = {0, 0, 0, 0, 0, 0};   // (Mx, My, Lx, Ly, xi, eta) of S_FTAB
+    double ftab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // (Mx, My, Lx, Ly, xi, eta, layout) of S_FTAB
     bool gtab_ready = false;                   // S_GTAB holds the E1 fit
     // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NUM_STAGES];
@@ -262,7 +262,8 @@ int finish_out(se2p_plan pl, const OutBuf &o)
 
 // dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32) -- 2D, batch grids;
 // 4 = Z2Z along y (batch contiguous rows of My); 5 = Z2Z along x of one
-// Mx x (My/2+1) half spectrum (stride My/2+1, My/2+1 transforms).
+// Mx x (My/2+1) half spectrum (stride My/2+1, My/2+1 transforms); 6 = Z2Z
+// along x of transposed half spectra (batch contiguous rows of Mx).
 int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, cufftHandle *h)
 {
     auto key = std::make_tuple(Mx, My, batch, dir);
@@ -278,6 +279,14 @@ int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, c
     if (dir == 4) {
         int ny = My;
         CKF(cufftPlanMany(&p, 1, &ny, nullptr, 1, My, nullptr, 1, My, CUFFT_Z2Z, batch));
+        CKF(cufftSetStream(p, st));
+        pl->ffts[key] = p;
+        *h = p;
+        return SE2P_OK;
+    }
+    if (dir == 6) {
+        int nx = Mx;
+        CKF(cufftPlanMany(&p, 1, &nx, nullptr, 1, Mx, nullptr, 1, Mx, CUFFT_Z2Z, batch));
         CKF(cufftSetStream(p, st));
         pl->ffts[key] = p;
         *h = p;
@@ -308,7 +317,8 @@ int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, c
 // keeps them between calls, like cuFFT keeps its twiddles.
 int filter_table(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
 {
-    const double key[6] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta};
+    const double key[7] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta,
+                           (double)fa.transposed};
     const size_t H = (size_t)fa.Mx * (fa.My / 2 + 1);
     const bool have = pl->buf[S_FTAB].p && pl->buf[S_FTAB].bytes >= H * sizeof(double2) &&
                       memcmp(key, pl->ftab_key, sizeof key) == 0;
@@ -763,17 +773,19 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         cufftDoubleComplex *zg = nullptr;
         CKS(ensure_t(pl, S_ZGRID, G * (size_t)std::max(ncg, npo), &zg));
         double2 *zgd = reinterpret_cast<double2 *>(zg);
+        // (the half spectra are kept transposed, [c][ky][x], so the x passes
+        // are contiguous batched rows like the y passes)
+        const int H1 = My / 2 + 1;
         cufftHandle fy, fx;
         CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
-        CKS(get_fft(pl, ks, Mx, My, 1, 5, &fx));
+        CKS(get_fft(pl, ks, Mx, My, nc * H1, 6, &fx));
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
             CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
             CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
-            CK(launch_split_half_spectra(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
-                                         pl->launches));
-            for (int c = 0; c < nc; c++)
-                CKF(cufftExecZ2Z(fx, spec + (size_t)c * H, spec + (size_t)c * H, CUFFT_FORWARD));
+            CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
+                                           pl->launches));
+            CKF(cufftExecZ2Z(fx, spec, spec, CUFFT_FORWARD));
         }
 
         FilterArgs fa;
@@ -790,6 +802,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.slp_out = 0;
         fa.dlp_out = J.slp ? 2 : 0;
         fa.etab = nullptr;
+        fa.transposed = 1;
         {
             StageTimer tm(pl, T_FILTER, ks);
             CKS(filter_table(pl, fa, ks));
@@ -797,15 +810,14 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         }
 
         // Z2D as 1D complex passes: C2C along x, Hermitian join, C2C along y, unpack
-        cufftHandle iy;
+        cufftHandle iy, ix;
         CKS(get_fft(pl, ks, Mx, My, npo * Mx, 4, &iy));
-        CKS(get_fft(pl, ks, Mx, My, 1, 5, &fx));
+        CKS(get_fft(pl, ks, Mx, My, nout * H1, 6, &ix));
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            for (int c = 0; c < nout; c++)
-                CKF(cufftExecZ2Z(fx, spec + (size_t)c * H, spec + (size_t)c * H, CUFFT_INVERSE));
-            CK(launch_join_half_spectra(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
-                                        pl->launches));
+            CKF(cufftExecZ2Z(ix, spec, spec, CUFFT_INVERSE));
+            CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
+                                          pl->launches));
             CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
             CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches));
         }

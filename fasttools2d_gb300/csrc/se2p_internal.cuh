@@ -305,6 +305,7 @@ struct FilterArgs {
     int slp_in, dlp_in;         // first spectrum of each kind (-1 = absent)
     int slp_out, dlp_out;       // where the 2 filtered spectra of each kind go
     const double2 *etab;        // per-mode (SLP e, DLP e*t) from k_filter_table, or NULL
+    int transposed = 0;         // spectra stored [c][ky][x] (x fastest) instead of [c][x][ky]
 };
 
 struct GatherArgs {
@@ -362,12 +363,12 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
 // Hermitian join, and the final real/imaginary unpack.
 cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,
                                    cudaStream_t st, int64_t &launches);
-cudaError_t launch_split_half_spectra(const double2 *z, int nc, int Mx, int My, double2 *spec,
-                                      cudaStream_t st, int64_t &launches);
-cudaError_t launch_join_half_spectra(const double2 *spec, int nout, int Mx, int My, double2 *z,
-                                     cudaStream_t st, int64_t &launches);
 cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
                                      cudaStream_t st, int64_t &launches);
+cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
+                                        cudaStream_t st, int64_t &launches);
+cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,
+                                       cudaStream_t st, int64_t &launches);
 // Real-space operator of a fixed geometry (se2p_geom.cu).
 cudaError_t launch_geom_rows(const RealArgs &a, bool slp, bool dlp, bool fill, int *rowcnt,
                              const int *rowptr, int *src, int *tgt, unsigned char *meta,

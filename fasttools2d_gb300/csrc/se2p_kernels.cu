@@ -1307,13 +1307,15 @@ template __global__ void k_spread<5>(SpreadArgs);
 // 2D real FFT as two 1D complex passes (FP64 form).
 //
 // cuFFT's batched 1D R2C of length 2688 runs at half the rate of its C2C of
-// the same length, so the real grids are transformed as complex pairs:
-// z = a + i b for grids (2p, 2p+1), C2C along y (contiguous rows), split by
-// Hermitian symmetry into the half spectra A(ky) = (Z(ky) + conj Z(-ky))/2,
-// B(ky) = (Z(ky) - conj Z(-ky))/(2i) for ky = 0..My/2, then C2C along x on
-// each half spectrum -- the D2Z result.  The inverse mirrors it: C2C along x,
-// Hermitian extension in ky and packing z = A + i B, C2C along y, real and
-// imaginary parts -- the Z2D result (unnormalised, as cuFFT's).
+// the same length, and its 2D plans run the second dimension strided, so the
+// real grids are transformed as complex pairs: z = a + i b for grids
+// (2p, 2p+1), C2C along y (contiguous rows), split by Hermitian symmetry into
+// the half spectra A(ky) = (Z(ky) + conj Z(-ky))/2, B(ky) = (Z(ky) -
+// conj Z(-ky))/(2i) for ky = 0..My/2, stored transposed ([c][ky][x]) so that
+// the C2C along x again runs on contiguous rows -- the D2Z result, transposed.
+// The inverse mirrors it: C2C along x, Hermitian extension in ky with the
+// transpose back and packing z = A + i B, C2C along y, real and imaginary
+// parts -- the Z2D result (unnormalised, as cuFFT's).
 // ===========================================================================
 __global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64_t G,
                                   double2 *__restrict__ z)
@@ -1330,48 +1332,6 @@ __global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64
     }
 }
 
-__global__ void k_split_half_spectra(const double2 *__restrict__ z, int nc, int Mx, int My,
-                                     double2 *__restrict__ spec)
-{
-    const int H1 = My / 2 + 1;
-    const int64_t H = (int64_t)Mx * H1, G = (int64_t)Mx * My;
-    const int64_t n = (int64_t)nc * H;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i / H);
-        const int64_t r = i - (int64_t)c * H;
-        const int x = (int)(r / H1), ky = (int)(r - (int64_t)x * H1);
-        const double2 *row = z + (int64_t)(c >> 1) * G + (int64_t)x * My;
-        const double2 zk = row[ky], zm = row[ky == 0 ? 0 : My - ky];
-        spec[i] = (c & 1) ? make_double2(0.5 * (zk.y + zm.y), 0.5 * (zm.x - zk.x))
-                          : make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
-    }
-}
-
-__global__ void k_join_half_spectra(const double2 *__restrict__ spec, int nout, int Mx, int My,
-                                    double2 *__restrict__ z)
-{
-    const int H1 = My / 2 + 1;
-    const int64_t H = (int64_t)Mx * H1, G = (int64_t)Mx * My;
-    const int npair = (nout + 1) / 2;
-    const int64_t n = (int64_t)npair * G;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int p = (int)(i / G);
-        const int64_t r = i - (int64_t)p * G;
-        const int x = (int)(r / My), ky = (int)(r - (int64_t)x * My);
-        const bool hi = ky > My / 2;
-        const int64_t src = (int64_t)x * H1 + (hi ? My - ky : ky);
-        double2 a = spec[(int64_t)(2 * p) * H + src];
-        double2 b = 2 * p + 1 < nout ? spec[(int64_t)(2 * p + 1) * H + src] : make_double2(0.0, 0.0);
-        if (hi) {
-            a.y = -a.y;
-            b.y = -b.y;
-        }
-        z[i] = make_double2(a.x - b.y, a.y + b.x);
-    }
-}
-
 __global__ void k_unpack_real_pairs(const double2 *__restrict__ z, int nout, int64_t G,
                                     double *__restrict__ grid)
 {
@@ -1384,6 +1344,79 @@ __global__ void k_unpack_real_pairs(const double2 *__restrict__ z, int nout, int
         const double2 v = z[i];
         grid[(int64_t)(2 * p) * G + e] = v.x;
         if (2 * p + 1 < nout) grid[(int64_t)(2 * p + 1) * G + e] = v.y;
+    }
+}
+
+// The same split and join with the half spectra stored transposed,
+// specT[c][ky][x] (x fastest), so that the x transforms run on contiguous
+// rows.  32 x 32 tiles through shared memory keep both sides coalesced.
+constexpr int kTT = 32;
+
+__global__ void __launch_bounds__(256) k_split_half_spectra_t(const double2 *__restrict__ z,
+                                                              int nc, int Mx, int My,
+                                                              double2 *__restrict__ specT)
+{
+    __shared__ double2 sa[kTT][kTT + 1], sb[kTT][kTT + 1];
+    const int H1 = My / 2 + 1;
+    const int64_t G = (int64_t)Mx * My, HT = (int64_t)H1 * Mx;
+    const int ky0 = blockIdx.x * kTT, x0 = blockIdx.y * kTT, p = blockIdx.z;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    const double2 *zp = z + (int64_t)p * G;
+    // load: lanes along ky
+    for (int r = ty; r < kTT; r += 8) {
+        const int x = x0 + r, ky = ky0 + tx;
+        if (x < Mx && ky < H1) {
+            const double2 zk = zp[(int64_t)x * My + ky];
+            const double2 zm = zp[(int64_t)x * My + (ky == 0 ? 0 : My - ky)];
+            sa[tx][r] = make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
+            sb[tx][r] = make_double2(0.5 * (zk.y + zm.y), 0.5 * (zm.x - zk.x));
+        }
+    }
+    __syncthreads();
+    // store: lanes along x
+    for (int r = ty; r < kTT; r += 8) {
+        const int ky = ky0 + r, x = x0 + tx;
+        if (x < Mx && ky < H1) {
+            specT[(int64_t)(2 * p) * HT + (int64_t)ky * Mx + x] = sa[r][tx];
+            if (2 * p + 1 < nc) specT[(int64_t)(2 * p + 1) * HT + (int64_t)ky * Mx + x] = sb[r][tx];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_join_half_spectra_t(const double2 *__restrict__ specT,
+                                                             int nout, int Mx, int My,
+                                                             double2 *__restrict__ z)
+{
+    __shared__ double2 sa[kTT][kTT + 1], sb[kTT][kTT + 1];
+    const int H1 = My / 2 + 1;
+    const int64_t G = (int64_t)Mx * My, HT = (int64_t)H1 * Mx;
+    const int ky0 = blockIdx.x * kTT, x0 = blockIdx.y * kTT, p = blockIdx.z;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const bool hasb = 2 * p + 1 < nout;
+    // load: lanes along x, one (mirrored) ky row per step
+    for (int r = ty; r < kTT; r += 8) {
+        const int ky = ky0 + r, x = x0 + tx;
+        if (x < Mx && ky < My) {
+            const bool hi = ky > My / 2;
+            const int64_t src = (int64_t)(hi ? My - ky : ky) * Mx + x;
+            double2 a = specT[(int64_t)(2 * p) * HT + src];
+            double2 b = hasb ? specT[(int64_t)(2 * p + 1) * HT + src] : make_double2(0.0, 0.0);
+            if (hi) {
+                a.y = -a.y;
+                b.y = -b.y;
+            }
+            sa[r][tx] = a;
+            sb[r][tx] = b;
+        }
+    }
+    __syncthreads();
+    // store: lanes along ky
+    for (int r = ty; r < kTT; r += 8) {
+        const int x = x0 + r, ky = ky0 + tx;
+        if (x < Mx && ky < My) {
+            const double2 a = sa[tx][r], b = sb[tx][r];
+            z[(int64_t)p * G + (int64_t)x * My + ky] = make_double2(a.x - b.y, a.y + b.x);
+        }
     }
 }
 
@@ -1461,7 +1494,14 @@ __global__ void k_filter(FilterArgs a)
     const int64_t G = (int64_t)a.Mx * H;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G) return;
-    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    int jx, jy;
+    if (a.transposed) {
+        jy = (int)(idx / a.Mx);
+        jx = (int)(idx - (int64_t)jy * a.Mx);
+    } else {
+        jx = (int)(idx / H);
+        jy = (int)(idx - (int64_t)jx * H);
+    }
     double2 *sp = reinterpret_cast<double2 *>(a.spec);
     const bool zero = (jx == 0 && jy == 0);
     const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
@@ -1519,7 +1559,14 @@ __global__ void k_filter_table(FilterArgs a, double2 *tab)
     const int64_t G = (int64_t)a.Mx * H;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G) return;
-    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    int jx, jy;
+    if (a.transposed) {
+        jy = (int)(idx / a.Mx);
+        jx = (int)(idx - (int64_t)jy * a.Mx);
+    } else {
+        jx = (int)(idx / H);
+        jy = (int)(idx - (int64_t)jx * H);
+    }
     const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
     const double K2 = k1 * k1 + k2 * k2;
     if (jx == 0 && jy == 0) {
@@ -1538,66 +1585,67 @@ __global__ void k_filter_table(FilterArgs a, double2 *tab)
 template <int NC, int PT>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs a)
 {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.nt) return;
-    const int P = PT > 0 ? PT : a.P;
-    const size_t G = (size_t)a.Mx * a.My;
-    const double2 T = a.tp[t];
-    int mx, my;
-    double px, py;
-    closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
-    const double ex = exp(a.a * (px * px + py * py + 2.0 * a.w * px));
-    const double e4y = exp(2.0 * a.a * a.w * py);
-    const double e3x = exp(-2.0 * a.a * a.h * px);
-    const double e3y = exp(-2.0 * a.a * a.h * py);
-    double wy[(PT > 0 ? PT : kMaxP) + 1];
-    {
-        double ey = 1.0;
-#pragma unroll
-        for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
-            if (j <= P) {
-                wy[j] = a.e1[j] * ey;
-                ey *= e3y;
-            }
-        }
-    }
-    double acc[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++) acc[c] = 0.0;
-    const bool rows_inside = my >= 0 && my + P < a.My;
-    double xf = ex * e4y;
-    for (int i = 0; i <= P; i++) {
-        const double *g = a.grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
-        double tc[NC];
-#pragma unroll
-        for (int c = 0; c < NC; c++) tc[c] = 0.0;
-        if (rows_inside) {
-            const double *gr = g + my;
-#pragma unroll
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nt;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int P = PT > 0 ? PT : a.P;
+        const size_t G = (size_t)a.Mx * a.My;
+        const double2 T = a.tp[t];
+        int mx, my;
+        double px, py;
+        closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
+        const double ex = exp(a.a * (px * px + py * py + 2.0 * a.w * px));
+        const double e4y = exp(2.0 * a.a * a.w * py);
+        const double e3x = exp(-2.0 * a.a * a.h * px);
+        const double e3y = exp(-2.0 * a.a * a.h * py);
+        double wy[(PT > 0 ? PT : kMaxP) + 1];
+        {
+            double ey = 1.0;
+    #pragma unroll
             for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
                 if (j <= P) {
-#pragma unroll
-                    for (int c = 0; c < NC; c++) tc[c] = fma(wy[j], __ldg(gr + c * G + j), tc[c]);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
-                if (j <= P) {
-                    const int row = wrap_index(my + j, a.My);
-#pragma unroll
-                    for (int c = 0; c < NC; c++) tc[c] = fma(wy[j], __ldg(g + c * G + row), tc[c]);
+                    wy[j] = a.e1[j] * ey;
+                    ey *= e3y;
                 }
             }
         }
-        const double wx = xf * a.e1[i];
-        xf *= e3x;
-#pragma unroll
-        for (int c = 0; c < NC; c++) acc[c] = fma(wx, tc[c], acc[c]);
+        double acc[NC];
+    #pragma unroll
+        for (int c = 0; c < NC; c++) acc[c] = 0.0;
+        const bool rows_inside = my >= 0 && my + P < a.My;
+        double xf = ex * e4y;
+        for (int i = 0; i <= P; i++) {
+            const double *g = a.grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
+            double tc[NC];
+    #pragma unroll
+            for (int c = 0; c < NC; c++) tc[c] = 0.0;
+            if (rows_inside) {
+                const double *gr = g + my;
+    #pragma unroll
+                for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                    if (j <= P) {
+    #pragma unroll
+                        for (int c = 0; c < NC; c++) tc[c] = fma(wy[j], __ldg(gr + c * G + j), tc[c]);
+                    }
+                }
+            } else {
+    #pragma unroll
+                for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                    if (j <= P) {
+                        const int row = wrap_index(my + j, a.My);
+    #pragma unroll
+                        for (int c = 0; c < NC; c++) tc[c] = fma(wy[j], __ldg(g + c * G + row), tc[c]);
+                    }
+                }
+            }
+            const double wx = xf * a.e1[i];
+            xf *= e3x;
+    #pragma unroll
+            for (int c = 0; c < NC; c++) acc[c] = fma(wx, tc[c], acc[c]);
+        }
+    #pragma unroll
+        for (int k = 0; k < NC / 2; k++)
+            a.out[k * a.nt + t] = make_double2(acc[2 * k] * a.scale, acc[2 * k + 1] * a.scale);
     }
-#pragma unroll
-    for (int k = 0; k < NC / 2; k++)
-        a.out[k * a.nt + t] = make_double2(acc[2 * k] * a.scale, acc[2 * k + 1] * a.scale);
 }
 
 template __global__ void k_gather<2, 24>(GatherArgs);
@@ -2072,7 +2120,9 @@ cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launche
 cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches)
 {
     if (a.nt <= 0) return cudaSuccess;
-    const unsigned g = grid_for(a.nt, 256);
+    // one resident block per SM, grid-stride over the sorted targets
+    unsigned g = grid_for(a.nt, 256);
+    if (g > (unsigned)sm_count()) g = (unsigned)sm_count();
     if (nc == 2) {
         if (a.P == 24) k_gather<2, 24><<<g, 256, 0, st>>>(a);
         else if (a.P == 12) k_gather<2, 12><<<g, 256, 0, st>>>(a);
@@ -2202,24 +2252,6 @@ cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_half_spectra(const double2 *z, int nc, int Mx, int My, double2 *spec,
-                                      cudaStream_t st, int64_t &launches)
-{
-    const int64_t n = (int64_t)nc * Mx * (My / 2 + 1);
-    k_split_half_spectra<<<stream_grid(n), 256, 0, st>>>(z, nc, Mx, My, spec);
-    launches++;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_join_half_spectra(const double2 *spec, int nout, int Mx, int My, double2 *z,
-                                     cudaStream_t st, int64_t &launches)
-{
-    const int64_t n = (int64_t)((nout + 1) / 2) * Mx * My;
-    k_join_half_spectra<<<stream_grid(n), 256, 0, st>>>(spec, nout, Mx, My, z);
-    launches++;
-    return cudaGetLastError();
-}
-
 cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
                                      cudaStream_t st, int64_t &launches)
 {
@@ -2237,6 +2269,29 @@ namespace se2p {
 cudaError_t launch_scan(const int *count, int n, int *start, cudaStream_t st, int64_t &launches)
 {
     k_scan<<<1, 1024, 0, st>>>(count, n, start);
+    launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace se2p
+
+namespace se2p {
+
+cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
+                                        cudaStream_t st, int64_t &launches)
+{
+    const int H1 = My / 2 + 1;
+    const dim3 g((H1 + kTT - 1) / kTT, (Mx + kTT - 1) / kTT, (nc + 1) / 2);
+    k_split_half_spectra_t<<<g, 256, 0, st>>>(z, nc, Mx, My, specT);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,
+                                       cudaStream_t st, int64_t &launches)
+{
+    const dim3 g((My + kTT - 1) / kTT, (Mx + kTT - 1) / kTT, (nout + 1) / 2);
+    k_join_half_spectra_t<<<g, 256, 0, st>>>(specT, nout, Mx, My, z);
     launches++;
     return cudaGetLastError();
 }
