@@ -792,9 +792,12 @@ template __global__ void k_real<true, true, kFormFF>(RealArgs);
 // ===========================================================================
 constexpr int kAdjVals = 7;   // gf1, gf2, gS11, gS1221, gS22, gy1, gy2
 
+constexpr int kAdjWarps = 4;   // warps per block of k_real_adj (shared memory per warp ~6.5 KB)
+
 struct AdjWarp {
     int2 q[2][64];
     double acc[kRing][kAdjVals + 1];
+    float2 accf[kRing][kAdjVals];    // the same from float-float pairs (FP64 form, queue 0)
     double2 pos[kRing];
     int box[kRing];
     long long idx[kRing];
@@ -823,6 +826,33 @@ __device__ __forceinline__ void seg_flush_n(Acc &accs, int lane, int key, double
         double *a = accs[key % kRing];
 #pragma unroll
         for (int i = 0; i < NV; i++) a[i] += v[i];
+    }
+    __syncwarp();
+}
+
+// seg_flush_n for float-float sums, into the float-float ring.
+template <int NV, class Acc>
+__device__ __forceinline__ void seg_flush_n_ff(Acc &accs, int lane, int key, float2 *v)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ko = __shfl_up_sync(~0u, key, o);
+        float2 a[NV];
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            a[i].x = __shfl_up_sync(~0u, v[i].x, o);
+            a[i].y = __shfl_up_sync(~0u, v[i].y, o);
+        }
+        if (lane >= o && ko == key) {
+#pragma unroll
+            for (int i = 0; i < NV; i++) v[i] = ff_add(v[i], a[i]);
+        }
+    }
+    const int kn = __shfl_down_sync(~0u, key, 1);
+    if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
+        float2 *a = accs[key % kRing];
+#pragma unroll
+        for (int i = 0; i < NV; i++) a[i] = ff_add(a[i], v[i]);
     }
     __syncwarp();
 }
@@ -990,10 +1020,10 @@ __device__ __forceinline__ void adj_pair_ff(const RealArgs &a, const AdjWarp &W,
 }
 
 template <bool SLP, bool DLP, int FORM>
-__global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
+__global__ void __launch_bounds__(kAdjWarps * 32) k_real_adj(RealArgs a)
 {
     constexpr bool FF = FORM == kFormFF;
-    __shared__ AdjWarp warps[kRealWarps];
+    __shared__ AdjWarp warps[kAdjWarps];
     __shared__ double tab[64];
     __shared__ float2 tabff[64];
     __shared__ double e1s[66];
@@ -1008,7 +1038,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
     // queue 0: far pairs (float-float in the FF form), queue 1: the rest in FP64
     const float xlo = FF ? 1.0001f : 1.0f, xhi = FF ? 63.9f : INFINITY;
     AdjWarp &W = warps[wid];
-    const int64_t nw = (int64_t)gridDim.x * kRealWarps;
+    const int64_t nw = (int64_t)gridDim.x * kAdjWarps;
     int head = 0, nfl = 0, gseq = 0;
     int qn[2] = {0, 0}, tag[2] = {-1, -1};
     long long enq[2] = {0, 0}, proc[2] = {0, 0};
@@ -1032,11 +1062,17 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
         const bool fl = tag[j] >= 0 && (lane >= cnt || tag[j] != eseq);
         const bool ffq = FF && j == 0;
         if (__any_sync(~0u, fl)) {
-            double tmp[kAdjVals];
+            if (ffq) {
+                float2 tf[kAdjVals];
 #pragma unroll
-            for (int i = 0; i < kAdjVals; i++)
-                tmp[i] = fl ? (ffq ? ff_to_double(vf[i]) : v[j][i]) : 0.0;
-            seg_flush_n<kAdjVals>(W.acc, lane, tag[j], tmp);
+                for (int i = 0; i < kAdjVals; i++) tf[i] = fl ? vf[i] : make_float2(0.f, 0.f);
+                seg_flush_n_ff<kAdjVals>(W.accf, lane, tag[j], tf);
+            } else {
+                double tmp[kAdjVals];
+#pragma unroll
+                for (int i = 0; i < kAdjVals; i++) tmp[i] = fl ? v[j][i] : 0.0;
+                seg_flush_n<kAdjVals>(W.acc, lane, tag[j], tmp);
+            }
             if (fl) {
 #pragma unroll
                 for (int i = 0; i < kAdjVals; i++) {
@@ -1055,7 +1091,11 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
     auto retire = [&](bool all) {
         while (nfl > 0 && (all || (proc[0] >= W.tend[0][head] + 32 &&
                                    proc[1] >= W.tend[1][head] + 32))) {
-            if (lane < kAdjVals) a.gout[kAdjVals * W.idx[head] + lane] = W.acc[head][lane];
+            if (lane < kAdjVals) {
+                double v = W.acc[head][lane];
+                if (FF) v += ff_to_double(W.accf[head][lane]);
+                a.gout[kAdjVals * W.idx[head] + lane] = v;
+            }
             head = (head + 1) % kRing;
             nfl--;
         }
@@ -1067,10 +1107,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
             batch(j, qn[j]);
             const int key = tag[j] >= 0 ? tag[j] : 0x7fffffff;
             if (FF && j == 0) {
-                double tmp[kAdjVals];
-#pragma unroll
-                for (int i = 0; i < kAdjVals; i++) tmp[i] = ff_to_double(vf[i]);
-                seg_flush_n<kAdjVals>(W.acc, lane, key, tmp);
+                seg_flush_n_ff<kAdjVals>(W.accf, lane, key, vf);
             } else {
                 seg_flush_n<kAdjVals>(W.acc, lane, key, v[j]);
             }
@@ -1085,7 +1122,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
     };
 
     // outer loop over forward sources (sorted), inner candidates are forward targets
-    for (int64_t s = (int64_t)blockIdx.x * kRealWarps + wid; s < a.nouter; s += nw) {
+    for (int64_t s = (int64_t)blockIdx.x * kAdjWarps + wid; s < a.nouter; s += nw) {
         if (nfl == kRing) drain();
         const int slot = (head + nfl) % kRing;
         nfl++;
@@ -1094,6 +1131,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real_adj(RealArgs a)
         const double2 Sp = a.sp[s];
         const float2 Sf = a.spf[s];
         if (lane < kAdjVals + 1) W.acc[slot][lane] = 0.0;
+        if (lane < kAdjVals) W.accf[slot][lane] = make_float2(0.f, 0.f);
         if (lane == 0) {
             W.pos[slot] = Sp;
             W.box[slot] = sbx;
@@ -2178,16 +2216,16 @@ template <int FORM>
 static void launch_real_adj_form(const RealArgs &a, bool slp, bool dlp, unsigned g,
                                  cudaStream_t st)
 {
-    if (slp && dlp) k_real_adj<true, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
-    else if (slp) k_real_adj<true, false, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
-    else k_real_adj<false, true, FORM><<<g, kRealWarps * 32, 0, st>>>(a);
+    if (slp && dlp) k_real_adj<true, true, FORM><<<g, kAdjWarps * 32, 0, st>>>(a);
+    else if (slp) k_real_adj<true, false, FORM><<<g, kAdjWarps * 32, 0, st>>>(a);
+    else k_real_adj<false, true, FORM><<<g, kAdjWarps * 32, 0, st>>>(a);
 }
 
 cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                             int64_t &launches, int form)
 {
     if (a.nouter <= 0) return cudaSuccess;
-    const int64_t want = (a.nouter + kRealWarps - 1) / kRealWarps;
+    const int64_t want = (a.nouter + kAdjWarps - 1) / kAdjWarps;
     const int64_t cap = (int64_t)sm_count() * 8;
     const unsigned g = (unsigned)(want < cap ? want : cap);
     if (form == kFormFF) launch_real_adj_form<kFormFF>(a, slp, dlp, g, st);
