@@ -404,6 +404,22 @@ def adjoint_leg(plan, steps, timed, dev):
             "fd_check": {"coords": 16, "h": h, "max_err_rel_to_max_grad": worst}}
 
 
+def aggregate_replicas(local_ms, steps, world, device=None):
+    """(max over ranks of a timed region in ms, whole-job evals/s).
+
+    Replicas: every rank evaluates its own copy of the workload, so the job
+    rate is world * steps over the slowest rank's time.  With world > 1 this
+    is an all-reduce (MAX) in the process group (NCCL on GPUs, gloo in the
+    CPU tests)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        local_ms = float(t.item())
+    return local_ms, world * steps / (local_ms * 1e-3)
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -458,11 +474,7 @@ def gpu_arm(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return aggregate_replicas(x, 1, world, dev)[0]
 
     for _ in range(args.warmup):
         step_device()
@@ -487,9 +499,8 @@ def gpu_arm(args, rank, world, local_rank):
     counts = plan.count_pairs(False, reset=True)
     stages = plan.stage_times(reset=True)
     plan.enable_timing(False)
-    total_ms = max_over_ranks(total_ms)
+    total_ms, value = aggregate_replicas(total_ms, args.steps, world, dev)
     ms_per_step = total_ms / args.steps
-    value = world * args.steps / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers ------------
     for _ in range(max(1, args.warmup // 2)):

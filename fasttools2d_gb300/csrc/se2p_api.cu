@@ -506,6 +506,45 @@ struct Io {
     int mode_slp = 0, mode_dlp = 1;   // k_assemble modes
 };
 
+// D2Z of nc real grids into transposed half spectra, as 1D complex passes:
+// pack pairs, C2C along y, Hermitian split (transposing), C2C along x.
+// zg holds ceil(nc/2) complex grids.
+static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const double *grid, int nc,
+                      cufftDoubleComplex *zg, cufftDoubleComplex *spec)
+{
+    const int H1 = My / 2 + 1, ncg = (nc + 1) / 2;
+    const size_t G = (size_t)Mx * My;
+    cufftHandle fy, fx;
+    CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
+    CKS(get_fft(pl, ks, Mx, My, nc * H1, 6, &fx));
+    double2 *zgd = reinterpret_cast<double2 *>(zg);
+    CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
+    CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
+    CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
+                                   pl->launches));
+    CKF(cufftExecZ2Z(fx, spec, spec, CUFFT_FORWARD));
+    return SE2P_OK;
+}
+
+// Z2D of nout transposed half spectra into real grids (the mirror of
+// fft_fwd_1d); zg holds ceil(nout/2) complex grids.
+static int fft_inv_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, cufftDoubleComplex *spec,
+                      int nout, cufftDoubleComplex *zg, double *grid)
+{
+    const int H1 = My / 2 + 1, npo = (nout + 1) / 2;
+    const size_t G = (size_t)Mx * My;
+    cufftHandle iy, ix;
+    CKS(get_fft(pl, ks, Mx, My, npo * Mx, 4, &iy));
+    CKS(get_fft(pl, ks, Mx, My, nout * H1, 6, &ix));
+    double2 *zgd = reinterpret_cast<double2 *>(zg);
+    CKF(cufftExecZ2Z(ix, spec, spec, CUFFT_INVERSE));
+    CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
+                                  pl->launches));
+    CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
+    CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches));
+    return SE2P_OK;
+}
+
 int run(se2p_plan pl, const Job &J, const Io &io)
 {
     DeviceGuard guard(pl->device);
@@ -772,20 +811,11 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         const int ncg = (nc + 1) / 2, npo = (nout + 1) / 2;
         cufftDoubleComplex *zg = nullptr;
         CKS(ensure_t(pl, S_ZGRID, G * (size_t)std::max(ncg, npo), &zg));
-        double2 *zgd = reinterpret_cast<double2 *>(zg);
         // (the half spectra are kept transposed, [c][ky][x], so the x passes
         // are contiguous batched rows like the y passes)
-        const int H1 = My / 2 + 1;
-        cufftHandle fy, fx;
-        CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
-        CKS(get_fft(pl, ks, Mx, My, nc * H1, 6, &fx));
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
-            CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
-            CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
-            CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
-                                           pl->launches));
-            CKF(cufftExecZ2Z(fx, spec, spec, CUFFT_FORWARD));
+            CKS(fft_fwd_1d(pl, ks, Mx, My, grid, nc, zg, spec));
         }
 
         FilterArgs fa;
@@ -810,16 +840,9 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         }
 
         // Z2D as 1D complex passes: C2C along x, Hermitian join, C2C along y, unpack
-        cufftHandle iy, ix;
-        CKS(get_fft(pl, ks, Mx, My, npo * Mx, 4, &iy));
-        CKS(get_fft(pl, ks, Mx, My, nout * H1, 6, &ix));
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            CKF(cufftExecZ2Z(ix, spec, spec, CUFFT_INVERSE));
-            CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
-                                          pl->launches));
-            CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
-            CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches));
+            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, grid));
         }
 
         GatherArgs ga;
@@ -1058,11 +1081,11 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
         StageTimer tm(pl, T_SPREAD, ks);
         CK(launch_spread(sa, 4, ks, pl->launches));
     }
-    cufftHandle fwd, inv;
-    CKS(get_fft(pl, ks, Mx, My, 4, 0, &fwd));
+    cufftDoubleComplex *zg = nullptr;
+    CKS(ensure_t(pl, S_ZGRID, G * 3, &zg));
     {
         StageTimer tm(pl, T_FFT_FWD, ks);
-        CKF(cufftExecD2Z(fwd, grid, spec));
+        CKS(fft_fwd_1d(pl, ks, Mx, My, grid, 4, zg, spec));
     }
     FilterArgs fa;
     fa.spec = spec;
@@ -1078,15 +1101,15 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     fa.dlp_in = 2;
     fa.dlp_out = 2;
     fa.etab = nullptr;
+    fa.transposed = 1;
     {
         StageTimer tm(pl, T_FILTER, ks);
         CKS(filter_table(pl, fa, ks));
         CK(launch_filter_adj(fa, ks, pl->launches));
     }
-    CKS(get_fft(pl, ks, Mx, My, 5, 1, &inv));
     {
         StageTimer tm(pl, T_FFT_INV, ks);
-        CKF(cufftExecZ2D(inv, spec, grid));
+        CKS(fft_inv_1d(pl, ks, Mx, My, spec, 5, zg, grid));
     }
     GatherAdjArgs ga;
     ga.sp = sp;

@@ -1724,7 +1724,14 @@ __global__ void k_filter_adj(FilterArgs a)
     const int64_t G = (int64_t)a.Mx * H;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G) return;
-    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    int jx, jy;
+    if (a.transposed) {
+        jy = (int)(idx / a.Mx);
+        jx = (int)(idx - (int64_t)jy * a.Mx);
+    } else {
+        jx = (int)(idx / H);
+        jy = (int)(idx - (int64_t)jx * H);
+    }
     double2 *sp = reinterpret_cast<double2 *>(a.spec);
     const bool zero = (jx == 0 && jy == 0);
     const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
