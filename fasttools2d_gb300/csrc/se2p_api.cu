@@ -43,6 +43,7 @@ enum Slot {
     S_ZGRID,                                    // complex pairs of grids (1D-pass FFT)
     S_GCOUNT, S_GTGT, S_GMETA,                  // geometry build scratch
     S_GCOEF, S_GCOEFF, S_GUR0, S_GUR1,          // geometry apply scratch
+    S_SBINS,                                    // fixed-point spread bound
     S_COUNT_SLOTS
 };
 
@@ -506,11 +507,56 @@ struct Io {
     int mode_slp = 0, mode_dlp = 1;   // k_assemble modes
 };
 
+// Spread with integer accumulation (k_spread_fix) when the source Gaussian's
+// x and y factors stay below 2^8: sets kY (2^kY bounds each factor) and kfac
+// (the factor of the bin bound).  The factors exceed 1 only when w differs
+// from h P/2; by at most exp(2 |a| h (h P/2 - w)).
+static bool spread_fixed_ok(const SpreadArgs &sa, int &kY, double &kfac, int &mult)
+{
+    const double wf = std::exp(-2.0 * sa.a * sa.h * std::max(0.0, sa.h * sa.P / 2 - sa.w));
+    if (!(wf <= 256.0)) return false;
+    kY = 0;
+    if (wf > 1.5) {
+        int e = 0;
+        std::frexp(wf, &e);                             // wf < 2^e
+        kY = e;
+    }
+    mult = ((sa.P + sa.Mx) / sa.Mx) * ((sa.P + sa.My) / sa.My);   // <= 16^2
+    kfac = std::ldexp((double)mult, 2 * kY);
+    return true;
+}
+
+// Runs the spread of nc components of sa.coef into sa.grid.  With *fixb set
+// on return, the grid holds k_spread_fix's integers or (when the bound slot
+// *fixb is all ones: crowded sources) the FP64 spread's doubles, and the pack
+// of fft_fwd_1d reads which; with *fixb null it holds doubles.
+static int spread(se2p_plan pl, SpreadArgs &sa, int nc, bool allow_fixed, cudaStream_t ks,
+                  const unsigned long long **fixb)
+{
+    int kY = 0, mult = 1;
+    double kfac = 1.0;
+    *fixb = nullptr;
+    sa.bound = nullptr;
+    if (allow_fixed && spread_fixed_ok(sa, kY, kfac, mult)) {
+        const int64_t nb = (int64_t)spread_bins(sa.Mx, sa.P) * spread_bins(sa.My, sa.P);
+        double *ws = nullptr;
+        CKS(ensure_t(pl, S_SBINS, 2 * (size_t)nb + 1, &ws));
+        sa.bound = reinterpret_cast<const unsigned long long *>(ws + nb);
+        CK(launch_spread_bound(sa, nc, kfac, mult, ws, ks, pl->launches));
+        CK(launch_spread_fix(sa, nc, kY, ks, pl->launches));
+        *fixb = sa.bound;
+    }
+    CK(launch_spread(sa, nc, ks, pl->launches));
+    return SE2P_OK;
+}
+
 // D2Z of nc real grids into transposed half spectra, as 1D complex passes:
 // pack pairs, C2C along y, Hermitian split (transposing), C2C along x.
-// zg holds ceil(nc/2) complex grids.
+// zg holds ceil(nc/2) complex grids.  With fixb the grids are the
+// fixed-point integers of k_spread_fix at the scale that *fixb gives.
 static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const double *grid, int nc,
-                      cufftDoubleComplex *zg, cufftDoubleComplex *spec)
+                      cufftDoubleComplex *zg, cufftDoubleComplex *spec,
+                      const unsigned long long *fixb)
 {
     const int H1 = My / 2 + 1, ncg = (nc + 1) / 2;
     const size_t G = (size_t)Mx * My;
@@ -518,7 +564,11 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
     CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
     CKS(get_fft(pl, ks, Mx, My, nc * H1, 6, &fx));
     double2 *zgd = reinterpret_cast<double2 *>(zg);
-    CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
+    if (fixb)
+        CK(launch_pack_fixed_pairs(reinterpret_cast<const long long *>(grid), nc, (int64_t)G, fixb,
+                                   zgd, ks, pl->launches));
+    else
+        CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
     CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
     CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
                                    pl->launches));
@@ -802,9 +852,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         sa.w = J.w;
         sa.a = -2 * J.xi * J.xi / J.eta;
         sa.e1 = e1;
+        const unsigned long long *fixb = nullptr;
         {
             StageTimer tm(pl, T_SPREAD, ks);
-            CK(launch_spread(sa, nc, ks, pl->launches));
+            CKS(spread(pl, sa, nc, pl->precision == SE2P_PRECISION_FP64, ks, &fixb));
         }
 
         // D2Z as 1D complex passes: pack pairs, C2C along y, split, C2C along x
@@ -815,7 +866,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         // are contiguous batched rows like the y passes)
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
-            CKS(fft_fwd_1d(pl, ks, Mx, My, grid, nc, zg, spec));
+            CKS(fft_fwd_1d(pl, ks, Mx, My, grid, nc, zg, spec, fixb));
         }
 
         FilterArgs fa;
@@ -1077,15 +1128,16 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     sa.w = J.w;
     sa.a = -2 * J.xi * J.xi / J.eta;
     sa.e1 = e1;
+    const unsigned long long *fixb = nullptr;
     {
         StageTimer tm(pl, T_SPREAD, ks);
-        CK(launch_spread(sa, 4, ks, pl->launches));
+        CKS(spread(pl, sa, 4, form == kFormFF, ks, &fixb));
     }
     cufftDoubleComplex *zg = nullptr;
     CKS(ensure_t(pl, S_ZGRID, G * 3, &zg));
     {
         StageTimer tm(pl, T_FFT_FWD, ks);
-        CKS(fft_fwd_1d(pl, ks, Mx, My, grid, 4, zg, spec));
+        CKS(fft_fwd_1d(pl, ks, Mx, My, grid, 4, zg, spec, fixb));
     }
     FilterArgs fa;
     fa.spec = spec;

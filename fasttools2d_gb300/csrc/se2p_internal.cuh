@@ -296,6 +296,10 @@ struct SpreadArgs {
     int Mx, My, P;
     double Lhx, Lhy, h, w, a;   // a = -2 xi^2 / eta
     const double *e1;     // exp(a h^2 j^2), j = -P/2..P/2
+    // Fixed-point form (k_spread_fix): the grids are int64 at scale 2^S, with S
+    // derived from *bound (the bit pattern of a positive double bounding
+    // every node's sum of |contributions|).
+    const unsigned long long *bound = nullptr;
 };
 
 struct FilterArgs {
@@ -402,6 +406,24 @@ cudaError_t launch_spread_f32(const SpreadArgsF &a, int nc, int sms, cudaStream_
 cudaError_t launch_filter_f32(const FilterArgsF &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_gather_f32(const GatherArgsF &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t &launches);
+// Fixed-point spread (se2p_kernels.cu): a bound on the grid values from
+// per-bin sums of |coefficients|, then int64 accumulation into a.grid
+// (reinterpreted as long long), and the pack that turns those grids into the
+// complex pairs of the forward FFT.
+// ws: 2 nb + 1 doubles, nb = spread_bins(Mx, P) * spread_bins(My, P): the
+// per-bin sums of max_c |c|, the bound slot at ws + nb, then nb int counts.
+// mult is the number of times one stencil can cover a node (> 1 when M <= P)
+// and kfac = mult 2^(2 kY).  When the bound slot ends up all ones the FP64
+// spread runs (launch it behind launch_spread_fix with a.bound set) and the
+// grids hold doubles.
+int spread_bins(int M, int P);
+cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mult, double *ws,
+                                cudaStream_t st, int64_t &launches);
+cudaError_t launch_spread_fix(const SpreadArgs &a, int nc, int kY, cudaStream_t st,
+                              int64_t &launches);
+cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
+                                    const unsigned long long *bound, double2 *z, cudaStream_t st,
+                                    int64_t &launches);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
                                 int64_t &launches);

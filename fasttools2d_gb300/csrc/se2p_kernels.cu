@@ -1261,6 +1261,8 @@ template __global__ void k_real_adj<true, true, kFormFF>(RealArgs);
 // atomics (executed in L2, off the SM's FP64 pipe).
 // ===========================================================================
 constexpr int kSpreadWarps = 8;
+// Bound-slot mark of the fixed-point spread (below): FP64 spread instead.
+constexpr unsigned long long kFixedOff = ~0ull;      // above every finite bound
 
 __device__ __forceinline__ int wrap_index(int i, int M)
 {
@@ -1271,6 +1273,8 @@ __device__ __forceinline__ int wrap_index(int i, int M)
 template <int NC>
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread(SpreadArgs a)
 {
+    // behind k_spread_fix: runs only when the bound slot says kFixedOff
+    if (a.bound && *a.bound != kFixedOff) return;
     __shared__ double wsh[kSpreadWarps][NC + 1][32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int P1 = a.P + 1, NN = P1 * P1;
@@ -1342,6 +1346,215 @@ template __global__ void k_spread<3>(SpreadArgs);
 template __global__ void k_spread<5>(SpreadArgs);
 
 // ===========================================================================
+// Fixed-point spread (FP64 form).
+//
+// The FP64 spread above is bound by the FP64 pipe (one DMUL per node and
+// component, 1.6 per clock per SM on GB300) and by FP64 atomics in L2.  Here
+// each contribution c Wx[i] Wy[j] is formed in integer arithmetic and added
+// with 64-bit integer atomics.  The source's Gaussian is split into its exact
+// x and y factors, X[i] = exp(a (px - h (i - P/2))^2) and the same for y, both
+// <= 1 when w = h P/2 (otherwise <= wf = exp(2 |a| h |w - h P/2|), which the
+// caller folds in as 2^kY).  The kernel stores Xc[i] = round(c X[i] 2^(S+3+kY))
+// and Y[j] = round(Y[j] 2^(62-kY)) as int64; the high 64 bits of Xc[i] Y[j]
+// are q = floor(2 c X Y 2^S), and the node receives (q + 1) >> 1, c X Y 2^S
+// rounded to the nearest integer.  (A plain floor would add a bias of -1/2
+// unit per contribution, which the k-space sums amplify where sources
+// cluster.)  The grid is int64 at scale 2^S, S chosen so that 2^S times a
+// bound on every node's sum of |contributions| is below 2^59: no partial sum
+// can overflow, the sum is exact and independent of the order of the atomics
+// (the grid is bitwise reproducible), and each contribution is off by at most
+// 3/4 unit of 2^-S, with no bias.
+//
+// The bound (k_spread_bin_sum, k_spread_bin_max): bins of at least P+2 nodes
+// per side hold the sums over their sources of max_c |c|.  A stencil reaches
+// P/2 nodes from its centre node, so a node receives only from sources of its
+// own bin and the 8 adjacent ones, and the largest 3 x 3 bin sum, times the
+// number of times one stencil covers a node when M <= P and times 2^(2 kY),
+// bounds every node's sum.
+//
+// The unit 2^-S is fixed by that bound, i.e. by sum |c|, while FP64 atomics
+// round relative to the partial sums, which grow like sqrt(n) when the signs
+// of the coefficients vary.  Each node's error is about n 2^-59 of its value
+// here against sqrt(n) 2^-53 there, n the number of stencils covering it: the
+// integer sums are the more accurate below n ~ 2^11 and lose beyond.  So when
+// some 3 x 3 bin neighbourhood holds more than kFixedMaxCover stencil covers,
+// k_spread_bin_max marks the bound slot kFixedOff, k_spread_fix returns at
+// once and the FP64 spread (launched behind it) runs instead; the pack reads
+// the same mark.  The choice costs no host synchronisation.
+// ===========================================================================
+constexpr int kFixedMaxCover = 1 << 14;
+
+// S with bound * 2^S < 2^59, from the bit pattern of the positive bound.
+__device__ __forceinline__ int fix_shift(unsigned long long bits)
+{
+    if (bits == kFixedOff) return 0;
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex == 0 || ex == 0x7ff) return 0;            // zero (no sources) or not finite
+    const int S = 59 - (ex - 1022);                  // bound < 2^(ex-1022)
+    return S < -960 ? -960 : (S > 960 ? 960 : S);
+}
+
+int spread_bins(int M, int P)
+{
+    const int b = M / (P + 2);
+    return b > 1 ? b : 1;
+}
+
+__global__ void k_spread_bin_sum(SpreadArgs a, int nc, int nbx, int nby, double *__restrict__ bins,
+                                 int *__restrict__ cnt)
+{
+    const double inv_h = 1.0 / a.h;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        double m = 0.0;
+        for (int c = 0; c < nc; c++) m = fmax(m, fabs(a.coef[(int64_t)nc * s + c]));
+        if (!(m > 0.0)) continue;
+        const double2 S = a.sp[s];
+        // the stencil's centre node, to within one node
+        const int cx = wrap_index((int)floor((S.x + a.Lhx) * inv_h), a.Mx);
+        const int cy = wrap_index((int)floor((S.y + a.Lhy) * inv_h), a.My);
+        const int bx = (int)((int64_t)cx * nbx / a.Mx), by = (int)((int64_t)cy * nby / a.My);
+        atomicAdd(&bins[(int64_t)bx * nby + by], m);
+        atomicAdd(&cnt[(int64_t)bx * nby + by], 1);
+    }
+}
+
+__global__ void k_spread_bin_max(const double *__restrict__ bins, const int *__restrict__ cnt,
+                                 int nbx, int nby, double kfac, int mult,
+                                 unsigned long long *__restrict__ bound)
+{
+    const int64_t nb = (int64_t)nbx * nby;
+    const int x0 = nbx >= 3 ? -1 : 0, x1 = nbx >= 2 ? 1 : 0;
+    const int y0 = nby >= 3 ? -1 : 0, y1 = nby >= 2 ? 1 : 0;
+    double best = 0.0;
+    int64_t crowd = 0;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        const int bx = (int)(b / nby), by = (int)(b - (int64_t)bx * nby);
+        double sum = 0.0;
+        int64_t n = 0;
+        for (int dx = x0; dx <= x1; dx++) {
+            const int ix = wrap_index(bx + dx, nbx);
+            for (int dy = y0; dy <= y1; dy++) {
+                const int64_t k = (int64_t)ix * nby + wrap_index(by + dy, nby);
+                sum += bins[k];
+                n += cnt[k];
+            }
+        }
+        best = fmax(best, sum);
+        crowd = max(crowd, n);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        best = fmax(best, __shfl_xor_sync(~0u, best, o));
+        crowd = max(crowd, __shfl_xor_sync(~0u, crowd, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (crowd * mult > kFixedMaxCover)
+            atomicMax(bound, kFixedOff);
+        else if (best > 0.0)      // positive doubles order as their bit patterns
+            atomicMax(bound, (unsigned long long)__double_as_longlong(best * kfac));
+    }
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix(SpreadArgs a, int kY)
+{
+    __shared__ long long xsh[kSpreadWarps][NC][32];
+    __shared__ long long ysh[kSpreadWarps][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P1 = a.P + 1, NN = P1 * P1;            // P1 <= 31
+    const size_t G = (size_t)a.Mx * a.My;
+    const unsigned long long bnd = *a.bound;
+    if (bnd == kFixedOff) return;                    // the FP64 spread runs instead
+    const int S = fix_shift(bnd);
+    const double sx = ldexp(1.0, S + 3 + kY), sy = ldexp(1.0, 62 - kY);
+    // (i, j) of flattened stencil entry q = lane + 32 k, stepped without division
+    const int di = 32 / P1, dj = 32 - di * P1, i0 = lane / P1, j0 = lane - i0 * P1;
+    const bool once = a.Mx > a.P && a.My > a.P;      // a stencil wraps at most once
+    long long *grid = reinterpret_cast<long long *>(a.grid);
+    const int64_t nw = (int64_t)gridDim.x * kSpreadWarps;
+    for (int64_t base = ((int64_t)blockIdx.x * kSpreadWarps + wid) * 32; base < a.ns;
+         base += nw * 32) {
+        const int64_t sl = base + lane;
+        int mx = 0, my = 0;
+        double Ax = 0.0, Ay = 0.0, e3x = 1.0, e3y = 1.0;
+        double cf[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) cf[c] = 0.0;
+        if (sl < a.ns) {
+            const double2 Sp = a.sp[sl];
+            double px, py;
+            closest_node(Sp.x, Sp.y, a.Lhx, a.Lhy, a.h, a.P, mx, my, px, py);
+            Ax = exp(a.a * (px * px + 2.0 * a.w * px)) * sx;
+            Ay = exp(a.a * (py * py + 2.0 * a.w * py)) * sy;
+            e3x = exp(-2.0 * a.a * a.h * px);
+            e3y = exp(-2.0 * a.a * a.h * py);
+#pragma unroll
+            for (int c = 0; c < NC; c++) cf[c] = a.coef[NC * sl + c];
+        }
+        const int cnt = (int)min((int64_t)32, a.ns - base);
+        for (int j = 0; j < cnt; j++) {
+            const int smx = __shfl_sync(~0u, mx, j), smy = __shfl_sync(~0u, my, j);
+            const double sAx = __shfl_sync(~0u, Ax, j), sAy = __shfl_sync(~0u, Ay, j);
+            const double b3x = __shfl_sync(~0u, e3x, j), b3y = __shfl_sync(~0u, e3y, j);
+            double px_ = lane >= 1 ? b3x : 1.0;
+            double py_ = lane >= 1 ? b3y : 1.0;
+            double sc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++) sc[c] = __shfl_sync(~0u, cf[c], j);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double tx = __shfl_up_sync(~0u, px_, o);
+                const double ty = __shfl_up_sync(~0u, py_, o);
+                if (lane >= o) {
+                    px_ *= tx;
+                    py_ *= ty;
+                }
+            }
+            if (lane < P1) {
+                const double e1v = a.e1[lane];
+                const double X = sAx * e1v * px_;
+#pragma unroll
+                for (int c = 0; c < NC; c++) xsh[wid][c][lane] = __double2ll_rn(sc[c] * X);
+                ysh[wid][lane] = __double2ll_rn(sAy * e1v * py_);
+            }
+            __syncwarp();
+            const int c0 = wrap_index(smx, a.Mx), r0 = wrap_index(smy, a.My);
+            int i = i0, jj = j0;
+            for (int qd = lane; qd < NN; qd += 32) {
+                int col = c0 + i, row = r0 + jj;
+                if (once) {
+                    col = col >= a.Mx ? col - a.Mx : col;
+                    row = row >= a.My ? row - a.My : row;
+                } else {
+                    col %= a.Mx;
+                    row %= a.My;
+                }
+                const long long y = ysh[wid][jj];
+                unsigned long long *g =
+                    reinterpret_cast<unsigned long long *>(grid + (size_t)col * a.My + row);
+#pragma unroll
+                for (int c = 0; c < NC; c++)
+                    atomicAdd(g + c * G,
+                              (unsigned long long)((__mul64hi(xsh[wid][c][i], y) + 1) >> 1));
+                i += di;
+                jj += dj;
+                if (jj >= P1) {
+                    jj -= P1;
+                    i++;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template __global__ void k_spread_fix<2>(SpreadArgs, int);
+template __global__ void k_spread_fix<3>(SpreadArgs, int);
+template __global__ void k_spread_fix<4>(SpreadArgs, int);
+template __global__ void k_spread_fix<5>(SpreadArgs, int);
+
+// ===========================================================================
 // 2D real FFT as two 1D complex passes (FP64 form).
 //
 // cuFFT's batched 1D R2C of length 2688 runs at half the rate of its C2C of
@@ -1355,8 +1568,8 @@ template __global__ void k_spread<5>(SpreadArgs);
 // transpose back and packing z = A + i B, C2C along y, real and imaginary
 // parts -- the Z2D result (unnormalised, as cuFFT's).
 // ===========================================================================
-__global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64_t G,
-                                  double2 *__restrict__ z)
+__device__ __forceinline__ void k_pack_real_pairs_body(const double *__restrict__ grid, int nc,
+                                                       int64_t G, double2 *__restrict__ z)
 {
     const int ncg = (nc + 1) / 2;
     const int64_t n = (int64_t)ncg * G;
@@ -1366,6 +1579,34 @@ __global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64
         const int64_t e = i - (int64_t)p * G;
         const double re = grid[(int64_t)(2 * p) * G + e];
         const double im = 2 * p + 1 < nc ? grid[(int64_t)(2 * p + 1) * G + e] : 0.0;
+        z[i] = make_double2(re, im);
+    }
+}
+
+__global__ void k_pack_real_pairs(const double *__restrict__ grid, int nc, int64_t G,
+                                  double2 *__restrict__ z)
+{
+    k_pack_real_pairs_body(grid, nc, G, z);
+}
+
+// The same pack from the fixed-point grids of k_spread_fix (value 2^-S v).
+__global__ void k_pack_fixed_pairs(const long long *__restrict__ grid, int nc, int64_t G,
+                                   const unsigned long long *__restrict__ bound,
+                                   double2 *__restrict__ z)
+{
+    if (*bound == kFixedOff) {                       // the grids hold doubles
+        k_pack_real_pairs_body(reinterpret_cast<const double *>(grid), nc, G, z);
+        return;
+    }
+    const double inv = ldexp(1.0, -fix_shift(*bound));
+    const int ncg = (nc + 1) / 2;
+    const int64_t n = (int64_t)ncg * G;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / G);
+        const int64_t e = i - (int64_t)p * G;
+        const double re = (double)grid[(int64_t)(2 * p) * G + e] * inv;
+        const double im = 2 * p + 1 < nc ? (double)grid[(int64_t)(2 * p + 1) * G + e] * inv : 0.0;
         z[i] = make_double2(re, im);
     }
 }
@@ -2287,6 +2528,52 @@ static unsigned stream_grid(int64_t n)
 {
     const int64_t want = (n + 255) / 256, cap = (int64_t)sm_count() * 16;
     return (unsigned)(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
+                                    const unsigned long long *bound, double2 *z, cudaStream_t st,
+                                    int64_t &launches)
+{
+    k_pack_fixed_pairs<<<stream_grid((int64_t)((nc + 1) / 2) * G), 256, 0, st>>>(grid, nc, G,
+                                                                                 bound, z);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mult, double *ws,
+                                cudaStream_t st, int64_t &launches)
+{
+    const int nbx = spread_bins(a.Mx, a.P), nby = spread_bins(a.My, a.P);
+    const int64_t nb = (int64_t)nbx * nby;
+    cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(double) * (2 * nb + 1), st);
+    if (e != cudaSuccess) return e;
+    unsigned long long *bound = reinterpret_cast<unsigned long long *>(ws + nb);
+    int *cnt = reinterpret_cast<int *>(ws + nb + 1);
+    if (a.ns > 0) {
+        k_spread_bin_sum<<<stream_grid(a.ns), 256, 0, st>>>(a, nc, nbx, nby, ws, cnt);
+        launches++;
+    }
+    k_spread_bin_max<<<stream_grid(nb), 256, 0, st>>>(ws, cnt, nbx, nby, kfac, mult, bound);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spread_fix(const SpreadArgs &a, int nc, int kY, cudaStream_t st,
+                              int64_t &launches)
+{
+    if (a.ns <= 0) return cudaSuccess;
+    const int64_t warps = (a.ns + 31) / 32;
+    const int64_t want = (warps + kSpreadWarps - 1) / kSpreadWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const unsigned g = (unsigned)(want < cap ? want : cap);
+    switch (nc) {
+    case 2: k_spread_fix<2><<<g, kSpreadWarps * 32, 0, st>>>(a, kY); break;
+    case 3: k_spread_fix<3><<<g, kSpreadWarps * 32, 0, st>>>(a, kY); break;
+    case 4: k_spread_fix<4><<<g, kSpreadWarps * 32, 0, st>>>(a, kY); break;
+    default: k_spread_fix<5><<<g, kSpreadWarps * 32, 0, st>>>(a, kY); break;
+    }
+    launches++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,

@@ -45,8 +45,11 @@ def test_both_forms_match_reference(ft, plans, name):
                                    g["Ly"], plan=plan)
         assert relerr(u, g["out_dlp_real"]) < PARITY, (plan.precision, "dlp")
     args = (g["Mx"], g["My"], g["Lx"], g["Ly"], g["w"], g["P"])
-    u = ft.mex_stokes_dlp_kspace(ps, pt, g["xi"], g["eta"], f, n, *args, plan=plans[1])
-    assert relerr(u, g["out_dlp_kspace"]) < PARITY
+    for plan in plans:
+        u = ft.mex_stokes_slp_kspace(ps, pt, g["xi"], g["eta"], f, *args, plan=plan)
+        assert relerr(u, g["out_slp_kspace"]) < PARITY, (plan.precision, "slp k")
+        u = ft.mex_stokes_dlp_kspace(ps, pt, g["xi"], g["eta"], f, n, *args, plan=plan)
+        assert relerr(u, g["out_dlp_kspace"]) < PARITY, (plan.precision, "dlp k")
 
 
 def _cloud(N, seed):
@@ -113,3 +116,75 @@ def test_ff_adjoint_agrees_with_native(ft, plans, N, xi, nside, M):
     for x, y in zip(a, b):
         assert relerr(x, y) < 1e-11, relerr(x, y)
         assert np.max(np.abs(x - y)) <= 1e-11 * np.max(np.abs(y))
+
+
+# --- fixed-point spread -----------------------------------------------------
+# The FP64 form spreads with 64-bit integer atomics on a grid at scale 2^S
+# (S from a bound on every node's sum of |contributions|); the FP64_NATIVE
+# form with FP64 atomics.  Both must give the same k-space sums to well
+# inside the 1e-12 parity bar, on inputs that stress the bound: clusters,
+# coefficients over 16 decades, w != h P/2 (Gaussian factors above 1) and
+# grids no wider than the stencil (a stencil covering a node several times).
+# Beyond 2^14 stencil covers in a 3 x 3 bin neighbourhood the FP64 form
+# switches to FP64 atomics on the device ("crowded" cases), where it agrees
+# with the native form to rounding.
+KSPACE_FIX_VS_NATIVE = 1e-13
+KSPACE_CROWDED_VS_NATIVE = 1e-14
+
+
+def _kspace_pair(ft, plans, p, q, f, n, xi, eta, M, w, P):
+    out = []
+    for plan in plans:
+        a = ft.mex_stokes_slp_kspace(p, q, xi, eta, f, M, M, 1.0, 1.0, w, P, plan=plan)
+        b = ft.mex_stokes_dlp_kspace(p, q, xi, eta, f, n, M, M, 1.0, 1.0, w, P, plan=plan)
+        out.append((a, b))
+    return out
+
+
+SPREAD_CASES = ["uniform", "clusters", "decades", "w_small", "grid_le_P", "crowded_grid_le_P",
+                "crowded_cluster"]
+
+
+def spread_case(case):
+    """Inputs of one fixed-point spread case: (p, q, f, n, xi, eta, M, w, P)."""
+    rng = np.random.default_rng(31)
+    N, xi, M, P = 30000, 60.0, 192, 24
+    if case == "grid_le_P":
+        N = 3000                                        # 4 covers per stencil: 12000 < 2^14
+    p, q, f, g, n = _cloud(N, 33)
+    eta = 0.8
+    h = 1.0 / M
+    w = h * P / 2
+    if case == "clusters":
+        c = rng.random((2, 8))
+        p = (c[:, rng.integers(0, 8, N)] + 0.002 * rng.standard_normal((2, N))) % 1.0
+    elif case == "crowded_cluster":
+        p = (0.5 + 0.001 * rng.standard_normal((2, N))) % 1.0
+    elif case == "decades":
+        f = f * 10.0 ** rng.uniform(-8, 8, N)
+    elif case == "w_small":
+        w = 0.7 * h * P / 2                             # x, y factors up to ~2^3
+    elif case in ("grid_le_P", "crowded_grid_le_P"):
+        M, P, xi = 16, 24, 4.0
+        w = (1.0 / M) * P / 2
+    return p, q, f, n, xi, eta, M, w, P
+
+
+@pytest.mark.parametrize("case", SPREAD_CASES)
+def test_fixed_spread_agrees_with_native(ft, plans, case):
+    p, q, f, n, xi, eta, M, w, P = spread_case(case)
+    (a1, b1), (a2, b2) = _kspace_pair(ft, plans, p, q, f, n, xi, eta, M, w, P)
+    assert np.all(np.isfinite(a1)) and np.all(np.isfinite(b1))
+    tol = KSPACE_CROWDED_VS_NATIVE if case.startswith("crowded") else KSPACE_FIX_VS_NATIVE
+    assert relerr(a1, a2) < tol, (case, "slp", relerr(a1, a2))
+    assert relerr(b1, b2) < tol, (case, "dlp", relerr(b1, b2))
+
+
+def test_fixed_spread_is_reproducible(ft, plans):
+    """Integer sums do not depend on the order of the atomics: the k-space
+    part of the FP64 form is the same bits on every call."""
+    ff = plans[0]
+    p, q, f, g, n = _cloud(50000, 41)
+    a = [ft.mex_stokes_dlp_kspace(p, q, 120.0, 0.8, f, n, 384, 384, 1.0, 1.0, 12 / 384, 24,
+                                  plan=ff) for _ in range(3)]
+    assert np.array_equal(a[0], a[1]) and np.array_equal(a[0], a[2])
