@@ -43,7 +43,7 @@ enum Slot {
     S_ZGRID,                                    // complex pairs of grids (1D-pass FFT)
     S_GCOUNT, S_GTGT, S_GMETA,                  // geometry build scratch
     S_GCOEF, S_GCOEFF, S_GUR0, S_GUR1,          // geometry apply scratch
-    S_SBINS,                                    // fixed-point spread bound
+    S_SBINS, S_GMAX,                            // fixed-point spread bound, gather scale
     S_COUNT_SLOTS
 };
 
@@ -526,6 +526,23 @@ static bool spread_fixed_ok(const SpreadArgs &sa, int &kY, double &kfac, int &mu
     return true;
 }
 
+// Bg of the fixed-point gather (k_gather_fix): 64 - log2(SX SY), SX = SY the
+// largest sum over a stencil row of the Gaussian factors
+// exp(a (p - h (i - P/2))^2), p in [0, h) (times wf >= 1 when w < h P/2).
+static int gather_fixed_bits(const SpreadArgs &sa)
+{
+    double sx = 0.0;
+    for (int i = 0; i <= sa.P; i++) {
+        const double c = sa.h * (i - sa.P / 2);
+        const double d = c < 0 ? -c : (c > sa.h ? c - sa.h : 0.0);
+        sx += std::exp(sa.a * d * d);
+    }
+    sx *= std::exp(-2.0 * sa.a * sa.h * std::max(0.0, sa.h * sa.P / 2 - sa.w));
+    int e = 0;
+    std::frexp(sx * sx, &e);                         // SX SY < 2^e
+    return std::min(62, 64 - e);
+}
+
 // Runs the spread of nc components of sa.coef into sa.grid.  With *fixb set
 // on return, the grid holds k_spread_fix's integers or (when the bound slot
 // *fixb is all ones: crowded sources) the FP64 spread's doubles, and the pack
@@ -579,7 +596,8 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
 // Z2D of nout transposed half spectra into real grids (the mirror of
 // fft_fwd_1d); zg holds ceil(nout/2) complex grids.
 static int fft_inv_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, cufftDoubleComplex *spec,
-                      int nout, cufftDoubleComplex *zg, double *grid)
+                      int nout, cufftDoubleComplex *zg, double *grid,
+                      unsigned long long *gmax = nullptr)
 {
     const int H1 = My / 2 + 1, npo = (nout + 1) / 2;
     const size_t G = (size_t)Mx * My;
@@ -591,7 +609,7 @@ static int fft_inv_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, cufftDouble
     CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
                                   pl->launches));
     CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
-    CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches));
+    CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches, gmax));
     return SE2P_OK;
 }
 
@@ -891,9 +909,23 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         }
 
         // Z2D as 1D complex passes: C2C along x, Hermitian join, C2C along y, unpack
+        // FP64 form: the fixed-point gather, whenever the spread could run
+        // fixed-point (the same Gaussian-factor condition)
+        unsigned long long *gmax = nullptr;
+        int Bg = 0;
+        {
+            int kY = 0, mult = 1;
+            double kfac = 1.0;
+            if (pl->precision == SE2P_PRECISION_FP64 && spread_fixed_ok(sa, kY, kfac, mult) &&
+                kY == 0) {
+                CKS(ensure_t(pl, S_GMAX, 1, &gmax));
+                CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long), ks));
+                Bg = gather_fixed_bits(sa);
+            }
+        }
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, grid));
+            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, grid, gmax));
         }
 
         GatherArgs ga;
@@ -913,7 +945,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ga.scale = s / (4 * kPi);
         ga.e1 = e1;
         ga.out = uk;
+        ga.gmax = gmax;
+        ga.Bg = Bg;
         StageTimer tm(pl, T_GATHER, ks);
+        if (gmax) CK(launch_grid_to_fixed(grid, (int64_t)nout * (int64_t)G, gmax, Bg, ks, pl->launches));
         CK(launch_gather(ga, nout, ks, pl->launches));
     }
 

@@ -320,6 +320,11 @@ struct GatherArgs {
     double Lhx, Lhy, h, w, a, scale;
     const double *e1;
     double2 *out;         // NC/2 outputs per target, [k * nt + t]
+    // Fixed-point form (k_gather_fix): *gmax holds the bit pattern of
+    // max |grid| (from the unpack), and launch_grid_to_fixed has turned the
+    // grids into int64 at the scale that gmax and Bg give.
+    const unsigned long long *gmax = nullptr;
+    int Bg = 0;
 };
 
 // FP32-grid (mixed precision) k-space arguments (se2p_kernels_f32.cu).
@@ -368,7 +373,13 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
 cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,
                                    cudaStream_t st, int64_t &launches);
 cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
-                                     cudaStream_t st, int64_t &launches);
+                                     cudaStream_t st, int64_t &launches,
+                                     unsigned long long *gmax = nullptr);
+// In place: the n doubles of grid become int64 round(g 2^Sg), max|g| 2^Sg < 2^Bg,
+// unless *gmax marks a non-finite value (then the grid stays as it is and
+// launch_gather runs the FP64 gather).
+cudaError_t launch_grid_to_fixed(double *grid, int64_t n, const unsigned long long *gmax, int Bg,
+                                 cudaStream_t st, int64_t &launches);
 cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
                                         cudaStream_t st, int64_t &launches);
 cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,

@@ -1263,6 +1263,8 @@ template __global__ void k_real_adj<true, true, kFormFF>(RealArgs);
 constexpr int kSpreadWarps = 8;
 // Bound-slot mark of the fixed-point spread (below): FP64 spread instead.
 constexpr unsigned long long kFixedOff = ~0ull;      // above every finite bound
+// Bit patterns of |g| at or above this are infinities and NaNs.
+constexpr unsigned long long kGridNonFinite = 0x7ff0000000000000ull;
 
 __device__ __forceinline__ int wrap_index(int i, int M)
 {
@@ -1400,14 +1402,22 @@ int spread_bins(int M, int P)
     return b > 1 ? b : 1;
 }
 
+// (A NaN or infinite coefficient marks the bound kFixedOff: the FP64 spread
+// carries it into the grid as the reference does.)
 __global__ void k_spread_bin_sum(SpreadArgs a, int nc, int nbx, int nby, double *__restrict__ bins,
-                                 int *__restrict__ cnt)
+                                 int *__restrict__ cnt, unsigned long long *__restrict__ bound)
 {
     const double inv_h = 1.0 / a.h;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.ns;
          s += (int64_t)gridDim.x * blockDim.x) {
         double m = 0.0;
-        for (int c = 0; c < nc; c++) m = fmax(m, fabs(a.coef[(int64_t)nc * s + c]));
+        bool finite = true;
+        for (int c = 0; c < nc; c++) {
+            const double v = fabs(a.coef[(int64_t)nc * s + c]);
+            finite = finite && v <= 1.7976931348623157e308;
+            m = fmax(m, v);
+        }
+        if (!finite) atomicMax(bound, kFixedOff);
         if (!(m > 0.0)) continue;
         const double2 S = a.sp[s];
         // the stencil's centre node, to within one node
@@ -1611,18 +1621,29 @@ __global__ void k_pack_fixed_pairs(const long long *__restrict__ grid, int nc, i
     }
 }
 
+// With gmax, also the largest |value| as a bit pattern (non-finite values
+// order above every finite one), for the fixed-point gather.
 __global__ void k_unpack_real_pairs(const double2 *__restrict__ z, int nout, int64_t G,
-                                    double *__restrict__ grid)
+                                    double *__restrict__ grid, unsigned long long *gmax)
 {
     const int npair = (nout + 1) / 2;
     const int64_t n = (int64_t)npair * G;
+    unsigned long long m = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int p = (int)(i / G);
         const int64_t e = i - (int64_t)p * G;
         const double2 v = z[i];
         grid[(int64_t)(2 * p) * G + e] = v.x;
-        if (2 * p + 1 < nout) grid[(int64_t)(2 * p + 1) * G + e] = v.y;
+        m = max(m, (unsigned long long)__double_as_longlong(fabs(v.x)));
+        if (2 * p + 1 < nout) {
+            grid[(int64_t)(2 * p + 1) * G + e] = v.y;
+            m = max(m, (unsigned long long)__double_as_longlong(fabs(v.y)));
+        }
+    }
+    if (gmax) {
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(~0u, m, o));
+        if ((threadIdx.x & 31) == 0 && m) atomicMax(gmax, m);
     }
 }
 
@@ -1864,6 +1885,8 @@ __global__ void k_filter_table(FilterArgs a, double2 *tab)
 template <int NC, int PT>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs a)
 {
+    // behind k_gather_fix: runs only when the grid held a non-finite value
+    if (a.gmax && *a.gmax < kGridNonFinite) return;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nt;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int P = PT > 0 ? PT : a.P;
@@ -1933,6 +1956,127 @@ template __global__ void k_gather<2, 12>(GatherArgs);
 template __global__ void k_gather<4, 12>(GatherArgs);
 template __global__ void k_gather<2, 0>(GatherArgs);
 template __global__ void k_gather<4, 0>(GatherArgs);
+
+// ===========================================================================
+// Fixed-point gather (FP64 form).
+//
+// The FP64 gather above issues one DFMA per stencil node and component and
+// is bound by the FP64 pipe.  Here the sums run in int64 registers.  After
+// the inverse FFT the grids become g' = round(g 2^Sg) (k_grid_to_fixed), Sg
+// chosen from the largest |g| so that |g'| < 2^Bg; the target's Gaussian
+// factors are Yq[j] = round(Y[j] 2^62) and Xq[i] = round(X[i] 2^62) with
+// X[i] = exp(a (px - h (i - P/2))^2) and Y the same in y, as in the fixed
+// spread.  A column sums the high 64 bits of g' Yq[j], floor(g Y 2^(Sg-2)),
+// and the target sums the high 64 bits of column * Xq[i]: sum g X Y at scale
+// 2^(Sg-4).  Each floor is off by -1/2 unit on average, which the sums take
+// back by starting from P/2 + 1 (P + 1 floors each).  Bg = 64 - log2(SX SY),
+// SX and SY the largest sums of the x and y factors over a stencil (host), so
+// no sum can overflow.  Every product is within one unit of 2^-(Sg-4), and a
+// unit is about SX SY 2^-60 max|g|: finer than the FP64 gather's roundings
+// relative to its partial sums unless max|g| is far above the grid values
+// near the target, which the normwise error measure does not see.
+// A NaN or infinity in the grid (non-finite inputs) sets gmax to a
+// non-finite pattern; then the grid stays double and the FP64 gather runs.
+// ===========================================================================
+
+// Sg with max|g| 2^Sg < 2^Bg, from the bit pattern of max|g|.
+__device__ __forceinline__ int grid_shift(unsigned long long gb, int Bg)
+{
+    if (gb == 0) return 0;
+    const int e = (int)((gb >> 52) & 0x7ff) - 1022;  // max|g| < 2^e
+    const int S = Bg - e;
+    return S < -960 ? -960 : (S > 960 ? 960 : S);
+}
+
+__global__ void k_grid_to_fixed(double *__restrict__ grid, int64_t n,
+                                const unsigned long long *__restrict__ gmax, int Bg)
+{
+    const unsigned long long gb = *gmax;
+    if (gb >= kGridNonFinite) return;
+    const double s = ldexp(1.0, grid_shift(gb, Bg));
+    long long *q = reinterpret_cast<long long *>(grid);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        q[i] = __double2ll_rn(grid[i] * s);
+}
+
+template <int NC, int PT>
+__global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
+{
+    const unsigned long long gb = *a.gmax;
+    if (gb >= kGridNonFinite) return;
+    const int P = PT > 0 ? PT : a.P;
+    const double outs = gb == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gb, a.Bg));
+    const long long bias = P / 2 + 1;
+    const long long *grid = reinterpret_cast<const long long *>(a.grid);
+    const size_t G = (size_t)a.Mx * a.My;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nt;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const double2 T = a.tp[t];
+        int mx, my;
+        double px, py;
+        closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
+        const double ax = exp(a.a * (px * px + 2.0 * a.w * px)) * 0x1p62;
+        const double ay = exp(a.a * (py * py + 2.0 * a.w * py)) * 0x1p62;
+        const double e3x = exp(-2.0 * a.a * a.h * px);
+        const double e3y = exp(-2.0 * a.a * a.h * py);
+        long long yq[(PT > 0 ? PT : kMaxP) + 1];
+        {
+            double ey = ay;
+#pragma unroll
+            for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                if (j <= P) {
+                    yq[j] = __double2ll_rn(a.e1[j] * ey);
+                    ey *= e3y;
+                }
+            }
+        }
+        long long acc[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) acc[c] = bias;
+        const bool rows_inside = my >= 0 && my + P < a.My;
+        double xf = ax;
+        for (int i = 0; i <= P; i++) {
+            const long long *g = grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
+            long long tc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++) tc[c] = bias;
+            if (rows_inside) {
+                const long long *gr = g + my;
+#pragma unroll
+                for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                    if (j <= P) {
+#pragma unroll
+                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                    if (j <= P) {
+                        const int row = wrap_index(my + j, a.My);
+#pragma unroll
+                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
+                    }
+                }
+            }
+            const long long xq = __double2ll_rn(xf * a.e1[i]);
+            xf *= e3x;
+#pragma unroll
+            for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
+        }
+#pragma unroll
+        for (int k = 0; k < NC / 2; k++)
+            a.out[k * a.nt + t] = make_double2((double)acc[2 * k] * outs, (double)acc[2 * k + 1] * outs);
+    }
+}
+template __global__ void k_gather_fix<2, 24>(GatherArgs);
+template __global__ void k_gather_fix<4, 24>(GatherArgs);
+template __global__ void k_gather_fix<2, 12>(GatherArgs);
+template __global__ void k_gather_fix<4, 12>(GatherArgs);
+template __global__ void k_gather_fix<2, 0>(GatherArgs);
+template __global__ void k_gather_fix<4, 0>(GatherArgs);
+
 
 // ===========================================================================
 // k-space adjoint.
@@ -2409,6 +2553,23 @@ cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t 
     // one resident block per SM, grid-stride over the sorted targets
     unsigned g = grid_for(a.nt, 256);
     if (g > (unsigned)sm_count()) g = (unsigned)sm_count();
+    if (a.gmax) {
+        // two resident blocks per SM (128 registers): the integer sums wait on
+        // loads, so they want more warps than the FP64-bound gather
+        const unsigned gf = std::min(grid_for(a.nt, 256), (unsigned)sm_count() * 2);
+        if (nc == 2) {
+            if (a.P == 24) k_gather_fix<2, 24><<<gf, 256, 0, st>>>(a);
+            else if (a.P == 12) k_gather_fix<2, 12><<<gf, 256, 0, st>>>(a);
+            else k_gather_fix<2, 0><<<gf, 256, 0, st>>>(a);
+        } else {
+            if (a.P == 24) k_gather_fix<4, 24><<<gf, 256, 0, st>>>(a);
+            else if (a.P == 12) k_gather_fix<4, 12><<<gf, 256, 0, st>>>(a);
+            else k_gather_fix<4, 0><<<gf, 256, 0, st>>>(a);
+        }
+        launches++;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     if (nc == 2) {
         if (a.P == 24) k_gather<2, 24><<<g, 256, 0, st>>>(a);
         else if (a.P == 12) k_gather<2, 12><<<g, 256, 0, st>>>(a);
@@ -2550,7 +2711,7 @@ cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mu
     unsigned long long *bound = reinterpret_cast<unsigned long long *>(ws + nb);
     int *cnt = reinterpret_cast<int *>(ws + nb + 1);
     if (a.ns > 0) {
-        k_spread_bin_sum<<<stream_grid(a.ns), 256, 0, st>>>(a, nc, nbx, nby, ws, cnt);
+        k_spread_bin_sum<<<stream_grid(a.ns), 256, 0, st>>>(a, nc, nbx, nby, ws, cnt, bound);
         launches++;
     }
     k_spread_bin_max<<<stream_grid(nb), 256, 0, st>>>(ws, cnt, nbx, nby, kfac, mult, bound);
@@ -2585,10 +2746,18 @@ cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double
 }
 
 cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
-                                     cudaStream_t st, int64_t &launches)
+                                     cudaStream_t st, int64_t &launches, unsigned long long *gmax)
 {
     k_unpack_real_pairs<<<stream_grid((int64_t)((nout + 1) / 2) * G), 256, 0, st>>>(z, nout, G,
-                                                                                    grid);
+                                                                                    grid, gmax);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_to_fixed(double *grid, int64_t n, const unsigned long long *gmax, int Bg,
+                                 cudaStream_t st, int64_t &launches)
+{
+    k_grid_to_fixed<<<stream_grid(n), 256, 0, st>>>(grid, n, gmax, Bg);
     launches++;
     return cudaGetLastError();
 }

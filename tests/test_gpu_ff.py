@@ -188,3 +188,15 @@ def test_fixed_spread_is_reproducible(ft, plans):
     a = [ft.mex_stokes_dlp_kspace(p, q, 120.0, 0.8, f, n, 384, 384, 1.0, 1.0, 12 / 384, 24,
                                   plan=ff) for _ in range(3)]
     assert np.array_equal(a[0], a[1]) and np.array_equal(a[0], a[2])
+
+
+def test_fixed_forms_carry_non_finite_values(ft, plans):
+    """A NaN force makes both forms' k-space sums non-finite at the same
+    places (the fixed-point spread and gather hand over to FP64 ones)."""
+    p, q, f, g, n = _cloud(5000, 43)
+    f = f.copy()
+    f[0, 17] = np.nan
+    a = [ft.mex_stokes_slp_kspace(p, q, 60.0, 0.8, f, 192, 192, 1.0, 1.0, 12 / 192, 24, plan=pl)
+         for pl in plans]
+    assert not np.all(np.isfinite(a[1]))
+    assert np.array_equal(np.isfinite(a[0]), np.isfinite(a[1]))
