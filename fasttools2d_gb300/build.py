@@ -21,7 +21,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libse2p.so")
-SOURCES = ["se2p_kernels.cu", "se2p_kernels_f32.cu", "se2p_geom.cu", "se2p_api.cu"]
+SOURCES = ["se2p_kernels.cu", "se2p_kernels_f32.cu", "se2p_fft_ff.cu", "se2p_geom.cu", "se2p_api.cu"]
 HEADERS = ["se2p_internal.cuh", "se2p_ff.cuh", os.path.join("..", "..", "include", "se2p.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",

@@ -44,6 +44,7 @@ enum Slot {
     S_GCOUNT, S_GTGT, S_GMETA,                  // geometry build scratch
     S_GCOEF, S_GCOEFF, S_GUR0, S_GUR1,          // geometry apply scratch
     S_SBINS, S_GMAX,                            // fixed-point spread bound, gather scale
+    S_TWY, S_TWX,                               // float-float FFT twiddles (y, x lengths)
     S_COUNT_SLOTS
 };
 
@@ -80,6 +81,11 @@ struct se2p_plan_st {
     bool count_pairs = false;
     double ftab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // (Mx, My, Lx, Ly, xi, eta, layout) of S_FTAB
     bool gtab_ready = false;                   // S_GTAB holds the E1 fit
+    // float-float FFT twiddles: the length and device copy each slot holds,
+    // and the host tables the (asynchronous) uploads read from
+    int tw_len[2] = {0, 0};
+    const void *tw_dev[2] = {nullptr, nullptr};
+    std::vector<float4> tw_host[2];
     // pending (start, end) event pairs per stage, resolved by se2p_plan_stage_times
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NUM_STAGES];
     double stage_ms[T_NUM_STAGES] = {0};
@@ -567,48 +573,88 @@ static int spread(se2p_plan pl, SpreadArgs &sa, int nc, bool allow_fixed, cudaSt
     return SE2P_OK;
 }
 
+// Twiddle table of the float-float row FFT of length L in slot S_TWY
+// (which = 0) or S_TWX (which = 1), built and uploaded once per length.
+static int fft_ff_table(se2p_plan pl, cudaStream_t st, int L, int which, const float4 **tw)
+{
+    float4 *d = nullptr;
+    CKS(ensure_t(pl, which ? S_TWX : S_TWY, (size_t)L, &d));
+    if (pl->tw_len[which] != L || pl->tw_dev[which] != d) {
+        std::vector<float4> &h = pl->tw_host[which];
+        h.resize((size_t)L);
+        fft_rows_ff_twiddles(L, h.data());
+        CK(cudaMemcpyAsync(d, h.data(), sizeof(float4) * (size_t)L, cudaMemcpyHostToDevice, st));
+        pl->tw_len[which] = L;
+        pl->tw_dev[which] = d;
+    }
+    *tw = d;
+    return SE2P_OK;
+}
+
+// The 1D passes in float-float (se2p_fft_ff.cu) when both lengths factor
+// into the supported radices; otherwise, and in the FP64_NATIVE form, cuFFT.
+static bool fft_ff_ok(int Mx, int My)
+{
+    FftRowsFF a, b;
+    return fft_rows_ff_plan(Mx, a) && fft_rows_ff_plan(My, b);
+}
+
+// One batch of 1D row transforms: cuFFT plan `dir` or the float-float rows.
+static int fft_rows(se2p_plan pl, cudaStream_t ks, bool ff, int Mx, int My, int L, int64_t rows,
+                    int dir, double2 *data, int sign)
+{
+    if (ff) {
+        FftRowsFF p;
+        fft_rows_ff_plan(L, p);
+        p.sign = sign;
+        const float4 *tw = nullptr;
+        CKS(fft_ff_table(pl, ks, L, L == My ? 0 : 1, &tw));
+        CK(launch_fft_rows_ff(data, rows, p, tw, ks, pl->launches));
+        return SE2P_OK;
+    }
+    cufftHandle h;
+    CKS(get_fft(pl, ks, Mx, My, (int)rows, dir, &h));
+    cufftDoubleComplex *z = reinterpret_cast<cufftDoubleComplex *>(data);
+    CKF(cufftExecZ2Z(h, z, z, sign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE));
+    return SE2P_OK;
+}
+
 // D2Z of nc real grids into transposed half spectra, as 1D complex passes:
 // pack pairs, C2C along y, Hermitian split (transposing), C2C along x.
 // zg holds ceil(nc/2) complex grids.  With fixb the grids are the
 // fixed-point integers of k_spread_fix at the scale that *fixb gives.
 static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const double *grid, int nc,
                       cufftDoubleComplex *zg, cufftDoubleComplex *spec,
-                      const unsigned long long *fixb)
+                      const unsigned long long *fixb, bool ff)
 {
     const int H1 = My / 2 + 1, ncg = (nc + 1) / 2;
     const size_t G = (size_t)Mx * My;
-    cufftHandle fy, fx;
-    CKS(get_fft(pl, ks, Mx, My, ncg * Mx, 4, &fy));
-    CKS(get_fft(pl, ks, Mx, My, nc * H1, 6, &fx));
     double2 *zgd = reinterpret_cast<double2 *>(zg);
     if (fixb)
         CK(launch_pack_fixed_pairs(reinterpret_cast<const long long *>(grid), nc, (int64_t)G, fixb,
                                    zgd, ks, pl->launches));
     else
         CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
-    CKF(cufftExecZ2Z(fy, zg, zg, CUFFT_FORWARD));
+    CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1));
     CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
                                    pl->launches));
-    CKF(cufftExecZ2Z(fx, spec, spec, CUFFT_FORWARD));
+    CKS(fft_rows(pl, ks, ff, Mx, My, Mx, (int64_t)nc * H1, 6, reinterpret_cast<double2 *>(spec), -1));
     return SE2P_OK;
 }
 
 // Z2D of nout transposed half spectra into real grids (the mirror of
 // fft_fwd_1d); zg holds ceil(nout/2) complex grids.
 static int fft_inv_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, cufftDoubleComplex *spec,
-                      int nout, cufftDoubleComplex *zg, double *grid,
+                      int nout, cufftDoubleComplex *zg, double *grid, bool ff,
                       unsigned long long *gmax = nullptr)
 {
     const int H1 = My / 2 + 1, npo = (nout + 1) / 2;
     const size_t G = (size_t)Mx * My;
-    cufftHandle iy, ix;
-    CKS(get_fft(pl, ks, Mx, My, npo * Mx, 4, &iy));
-    CKS(get_fft(pl, ks, Mx, My, nout * H1, 6, &ix));
     double2 *zgd = reinterpret_cast<double2 *>(zg);
-    CKF(cufftExecZ2Z(ix, spec, spec, CUFFT_INVERSE));
+    CKS(fft_rows(pl, ks, ff, Mx, My, Mx, (int64_t)nout * H1, 6, reinterpret_cast<double2 *>(spec), 1));
     CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
                                   pl->launches));
-    CKF(cufftExecZ2Z(iy, zg, zg, CUFFT_INVERSE));
+    CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)npo * Mx, 4, zgd, 1));
     CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches, gmax));
     return SE2P_OK;
 }
@@ -875,6 +921,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             StageTimer tm(pl, T_SPREAD, ks);
             CKS(spread(pl, sa, nc, pl->precision == SE2P_PRECISION_FP64, ks, &fixb));
         }
+        const bool ffft = pl->precision == SE2P_PRECISION_FP64 && fft_ff_ok(Mx, My);
 
         // D2Z as 1D complex passes: pack pairs, C2C along y, split, C2C along x
         const int ncg = (nc + 1) / 2, npo = (nout + 1) / 2;
@@ -884,7 +931,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         // are contiguous batched rows like the y passes)
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
-            CKS(fft_fwd_1d(pl, ks, Mx, My, grid, nc, zg, spec, fixb));
+            CKS(fft_fwd_1d(pl, ks, Mx, My, grid, nc, zg, spec, fixb, ffft));
         }
 
         FilterArgs fa;
@@ -925,7 +972,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         }
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, grid, gmax));
+            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, grid, ffft, gmax));
         }
 
         GatherArgs ga;
@@ -1168,11 +1215,12 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
         StageTimer tm(pl, T_SPREAD, ks);
         CKS(spread(pl, sa, 4, form == kFormFF, ks, &fixb));
     }
+    const bool ffft = form == kFormFF && fft_ff_ok(Mx, My);
     cufftDoubleComplex *zg = nullptr;
     CKS(ensure_t(pl, S_ZGRID, G * 3, &zg));
     {
         StageTimer tm(pl, T_FFT_FWD, ks);
-        CKS(fft_fwd_1d(pl, ks, Mx, My, grid, 4, zg, spec, fixb));
+        CKS(fft_fwd_1d(pl, ks, Mx, My, grid, 4, zg, spec, fixb, ffft));
     }
     FilterArgs fa;
     fa.spec = spec;
@@ -1196,7 +1244,7 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     }
     {
         StageTimer tm(pl, T_FFT_INV, ks);
-        CKS(fft_inv_1d(pl, ks, Mx, My, spec, 5, zg, grid));
+        CKS(fft_inv_1d(pl, ks, Mx, My, spec, 5, zg, grid, ffft));
     }
     GatherAdjArgs ga;
     ga.sp = sp;

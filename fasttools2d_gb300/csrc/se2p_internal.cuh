@@ -384,6 +384,20 @@ cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My
                                         cudaStream_t st, int64_t &launches);
 cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,
                                        cudaStream_t st, int64_t &launches);
+// Float-float row FFTs (se2p_fft_ff.cu): unnormalised C2C of `rows`
+// contiguous rows of L complex doubles, in place, sign -1 forward / +1
+// inverse (cuFFT's convention).  Lengths 8^a 4^b 2^c 7^d 5^e 3^f up to
+// kFftFFMaxLen; fft_rows_ff_plan says whether L is one.
+constexpr int kFftFFMaxLen = 6144;
+constexpr int kFftFFMaxStages = 16;
+struct FftRowsFF {
+    int L = 0, nst = 0, sign = -1;
+    int radix[kFftFFMaxStages] = {};
+};
+bool fft_rows_ff_plan(int L, FftRowsFF &p);
+void fft_rows_ff_twiddles(int L, float4 *host);   // exp(-2 pi i m/L), m < L, float-float
+cudaError_t launch_fft_rows_ff(double2 *data, int64_t rows, const FftRowsFF &p, const float4 *tw,
+                               cudaStream_t st, int64_t &launches);
 // Real-space operator of a fixed geometry (se2p_geom.cu).
 cudaError_t launch_geom_rows(const RealArgs &a, bool slp, bool dlp, bool fill, int *rowcnt,
                              const int *rowptr, int *src, int *tgt, unsigned char *meta,
