@@ -1275,7 +1275,7 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     if (side) CK(cudaStreamWaitEvent(st, pl->join, 0));
 
     double2 *part = nullptr;
-    CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
+    CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts + 1, &part));
     {
         StageTimer tm(pl, T_ASSEMBLE);
         CK(launch_adj_assemble(ns, sperm, gr, gk, wcoef, nt, part, ps, dlp ? fd : zeros,

@@ -13,7 +13,8 @@
 // 1e-12 parity bound (the systematic errors of float-float Gaussian weights
 // do not average out, which is why the spread and gather stay exact).
 //
-// One CTA per row: the row is read as doubles, scaled by a power of two that
+// One CTA per row: the row is read once as doubles (staged in shared memory
+// for the exponent scan), scaled by a power of two that
 // puts its largest entry near 2^64 (exact; the FFT of a row of L <= 2^13
 // values grows it by at most L), split into float-float pairs with integer
 // operations, transformed by mixed-radix Stockham stages (radices 8, 4, 2,
@@ -78,17 +79,23 @@ __device__ __forceinline__ fc tw_load(const float4 *tw, int m, float s)
                    : fc{make_float2(t.x, t.y), make_float2(-t.z, -t.w)};
 }
 
-// Shared buffer: four float arrays of L (re hi, re lo, im hi, im lo).
-__device__ __forceinline__ fc sh_get(const float *b, int L, int k)
+// Shared buffer: four float arrays (re hi, re lo, im hi, im lo) of Lp =
+// sh_len(L) words each, element k at k + k/32: the padding word per 32 turns
+// the stride-R stores of the early stages (R = 2, 4, 8) into at most 2-way
+// bank conflicts.
+__host__ __device__ __forceinline__ int sh_len(int L) { return L + (L >> 5) + 1; }
+__device__ __forceinline__ fc sh_get(const float *b, int Lp, int k)
 {
-    return {make_float2(b[k], b[L + k]), make_float2(b[2 * L + k], b[3 * L + k])};
+    k += k >> 5;
+    return {make_float2(b[k], b[Lp + k]), make_float2(b[2 * Lp + k], b[3 * Lp + k])};
 }
-__device__ __forceinline__ void sh_put(float *b, int L, int k, const fc &v)
+__device__ __forceinline__ void sh_put(float *b, int Lp, int k, const fc &v)
 {
+    k += k >> 5;
     b[k] = v.r.x;
-    b[L + k] = v.r.y;
-    b[2 * L + k] = v.i.x;
-    b[3 * L + k] = v.i.y;
+    b[Lp + k] = v.r.y;
+    b[2 * Lp + k] = v.i.x;
+    b[3 * Lp + k] = v.i.y;
 }
 
 // Radix-R butterflies of one Stockham stage.  Input element r of butterfly j
@@ -197,12 +204,12 @@ __device__ void stage(const float *A, float *B, int L, int Ns, float s, const fl
             cst[m - 1] = {w.r, ff_neg(w.i)};
         }
     }
-    const int nb = L / R, stride = L / (Ns * R);
+    const int nb = L / R, stride = L / (Ns * R), Lp = sh_len(L);
     for (int j = threadIdx.x; j < nb; j += blockDim.x) {
         const int k = j % Ns;
         fc v[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = sh_get(A, L, j + r * nb);
+        for (int r = 0; r < R; r++) v[r] = sh_get(A, Lp, j + r * nb);
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; r++) v[r] = fc_mul(v[r], tw_load(tw, k * r * stride, s));
@@ -210,7 +217,7 @@ __device__ void stage(const float *A, float *B, int L, int Ns, float s, const fl
         dft<R>(v, s, cst);
         const int o = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) sh_put(B, L, o + r * Ns, v[r]);
+        for (int r = 0; r < R; r++) sh_put(B, Lp, o + r * Ns, v[r]);
     }
 }
 
@@ -266,15 +273,18 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
 {
     extern __shared__ float fsh[];
     __shared__ int emax_w[8];
-    const int L = p.L;
+    const int L = p.L, Lp = sh_len(L);
     const float s = (float)p.sign;
-    float *A = fsh, *B = fsh + 4 * L;
+    float *A = fsh, *B = fsh + 4 * Lp;
     for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
         double2 *d = data + row * L;
-        // largest exponent of the row
+        // the row as doubles into B (4 Lp floats >= L double2), and its
+        // largest exponent
+        double2 *raw = reinterpret_cast<double2 *>(B);
         int em = 0;
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
             const double2 v = d[k];
+            raw[k] = v;
             em = max(em, max((__double2hiint(v.x) >> 20) & 0x7ff, (__double2hiint(v.y) >> 20) & 0x7ff));
         }
         for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(~0u, em, o));
@@ -287,8 +297,8 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
         // spreads through the row as in an FP64 transform)
         const int e = (em == 0 || em == 0x7ff) ? 0 : em - 1023 - 63;
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const double2 v = d[k];
-            sh_put(A, L, k, fc{ff_split_scaled(v.x, e), ff_split_scaled(v.y, e)});
+            const double2 v = raw[k];
+            sh_put(A, Lp, k, fc{ff_split_scaled(v.x, e), ff_split_scaled(v.y, e)});
         }
         __syncthreads();
         int Ns = 1;
@@ -309,13 +319,13 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
             __syncthreads();
         }
         for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const fc v = sh_get(A, L, k);
+            const fc v = sh_get(A, Lp, k);
             d[k] = make_double2(ff_to_double_scaled(v.r.x, v.r.y, e),
                                 ff_to_double_scaled(v.i.x, v.i.y, e));
         }
         // the next row reuses both buffers and emax_w
         A = fsh;
-        B = fsh + 4 * L;
+        B = fsh + 4 * Lp;
         __syncthreads();
     }
 }
@@ -351,7 +361,7 @@ cudaError_t launch_fft_rows_ff(double2 *data, int64_t rows, const FftRowsFF &p, 
                                cudaStream_t st, int64_t &launches)
 {
     if (rows <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * 8 * (size_t)p.L;
+    const size_t smem = sizeof(float) * 8 * (size_t)sh_len(p.L);
     cudaError_t e = cudaFuncSetAttribute(k_fft_rows_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

@@ -526,7 +526,9 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         tabff[i] = ff_split(c_exp_tab[i]);
     }
     const float2 xi2ff = ff_split(a.xi2), pfff = ff_split(a.pf);
-    // float-float pairs: 1 < x < 64 with margins for the FP32 pre-test
+    // Queue 0 (the fast pairs): float-float pairs 1 < x < 64 with margins
+    // for the FP32 pre-test; FP32-grid form, x > 1 (near pairs, E1 at small
+    // argument, stay FP64 in both forms).
     const float xlo = FF ? 1.0001f : 1.0f, xhi = FF ? 63.9f : INFINITY;
     for (int i = threadIdx.x; i < 66; i += blockDim.x) {
         e1s[i] = (&c_e1[0][0])[i];
@@ -2203,21 +2205,24 @@ __global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
     double xf = ex * e4y;
     for (int i = 0; i <= P; i++) {
         const double *g = a.grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
-        double tc[5] = {0, 0, 0, 0, 0}, u = 0.0;
+        // per component the column sums with wy and wyd (10 DFMA per node);
+        // the wyd sums meet the coefficients once per column
+        double tc[5] = {0, 0, 0, 0, 0}, td[5] = {0, 0, 0, 0, 0};
 #pragma unroll
         for (int j = 0; j < PM; j++) {
             if (j <= P) {
                 const int row = rows_inside ? my + j : wrap_index(my + j, a.My);
-                double cp = 0.0;
 #pragma unroll
                 for (int k = 0; k < 5; k++) {
                     const double v = __ldg(g + k * G + row);
                     tc[k] = fma(wy[j], v, tc[k]);
-                    cp = fma(c[k], v, cp);
+                    td[k] = fma(wyd[j], v, td[k]);
                 }
-                u = fma(wyd[j], cp, u);
             }
         }
+        double u = 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) u = fma(c[k], td[k], u);
         const double wx = xf * a.e1[i];
         const double wxd = wx * 2.0 * a.a * (px + a.w - a.h * i);
         xf *= e3x;
@@ -2239,6 +2244,7 @@ __global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
 
 template __global__ void k_gather_adj<24>(GatherAdjArgs);
 template __global__ void k_gather_adj<0>(GatherAdjArgs);
+
 
 // sum_t w_dlp(t) (the zero-mode term's weight), partial sums per block.
 __global__ void __launch_bounds__(256) k_wsum_part(int64_t n, const double *__restrict__ w,
@@ -2268,12 +2274,24 @@ __global__ void __launch_bounds__(256) k_wsum_part(int64_t n, const double *__re
     }
 }
 
+// part[nparts] = the sum of part[0 .. nparts-1], added in index order.
+__global__ void k_wsum_final(int nparts, double2 *__restrict__ part)
+{
+    if (threadIdx.x != 0) return;
+    double2 t = make_double2(0.0, 0.0);
+    for (int b = 0; b < nparts; b++) {
+        t.x += part[b].x;
+        t.y += part[b].y;
+    }
+    part[nparts] = t;
+}
+
 // Combine the real-space (gr, 7 per sorted source, unscaled) and k-space (gk,
 // 7 per sorted source, scaled) adjoint parts with the DLP zero-mode term and
 // the chain rule S = f (x) n; write gradients in the caller's source order.
 __global__ void k_adj_assemble(int64_t n, const int *__restrict__ perm,
                                const double *__restrict__ gr, const double *__restrict__ gk,
-                               const double2 *__restrict__ part, int nparts,
+                               const double2 *__restrict__ wsum,
                                const double2 *__restrict__ praw, const double2 *__restrict__ fd,
                                const double2 *__restrict__ nrm, double inv_area, int slp, int dlp,
                                double2 *__restrict__ g_pos, double2 *__restrict__ g_fs,
@@ -2287,11 +2305,7 @@ __global__ void k_adj_assemble(int64_t n, const int *__restrict__ perm,
     double gp1 = r[5] * q + k[5], gp2 = r[6] * q + k[6];
     if (slp && g_fs) g_fs[i] = make_double2(r[0] * q + k[0], r[1] * q + k[1]);
     if (dlp) {
-        double Wx = 0.0, Wy = 0.0;
-        for (int b = 0; b < nparts; b++) {
-            Wx += part[b].x;
-            Wy += part[b].y;
-        }
+        const double Wx = wsum->x, Wy = wsum->y;
         const double2 x = praw[i], f = fd[i], m = nrm[i];
         const double zw = (Wx * x.x + Wy * x.y) * inv_area;        // d J / d (f.n)
         const double gS11 = -r[2] * q + k[2] + zw, gS12 = -r[3] * q + k[3];
@@ -2670,10 +2684,11 @@ cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, co
 {
     if (dlp) {
         k_wsum_part<<<kZeroModeParts, 256, 0, st>>>(nt, w, 4, 2, part);
-        launches++;
+        k_wsum_final<<<1, 32, 0, st>>>(kZeroModeParts, part);
+        launches += 2;
     }
     if (n > 0) {
-        k_adj_assemble<<<grid_for(n, 256), 256, 0, st>>>(n, perm, gr, gk, part, kZeroModeParts,
+        k_adj_assemble<<<grid_for(n, 256), 256, 0, st>>>(n, perm, gr, gk, part + kZeroModeParts,
                                                          praw, fd, nrm, inv_area, slp, dlp,
                                                          g_pos, g_fs, g_fd, g_n);
         launches++;

@@ -82,3 +82,27 @@ def test_overlap_switch_gives_same_result(ft):
     b = ft.stokes_ewald(p, q, f, g, n, prm, plan=plan)
     assert relerr(a[0], b[0]) < 1e-13 and relerr(a[1], b[1]) < 1e-13
     plan.close()
+
+
+def test_fp32grid_real_space_close_pairs(ft):
+    """Clusters and near-coincident pairs (r = 1e-6, 1e-7, 1e-9) with targets
+    on the sources (self terms): real space against the oracle."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(23)
+    c = rng.random((2, 30))
+    p = (c[:, rng.integers(0, 30, 3000)] + 0.003 * rng.standard_normal((2, 3000))) % 1.0
+    p = np.hstack([p, p[:, :40] + 1e-6, p[:, 40:80] + 1e-7, p[:, 80:120] + 1e-9])
+    N = p.shape[1]
+    f = rng.standard_normal((2, N))
+    th = rng.random(N) * 2 * np.pi
+    n = np.vstack([np.cos(th), np.sin(th)])
+    plan = ft.Plan(0)
+    plan.set_precision("fp32_grid")
+    xi, ns = 40.0, 8
+    a = ft.mex_stokes_slp_real(p, p, f, xi, ns, ns, 1.0, 1.0, plan=plan)
+    b = ft.mex_stokes_dlp_real(p, p, f, n, xi, ns, ns, 1.0, 1.0, plan=plan)
+    ra = O.mex_stokes_slp_real(p, p, f, xi, ns, ns, 1.0, 1.0)
+    rb = O.mex_stokes_dlp_real(p, p, f, n, xi, ns, ns, 1.0, 1.0)
+    assert relerr(a, ra) < 2e-6 and _rms(a, ra) < 1e-6, (relerr(a, ra), _rms(a, ra))
+    assert relerr(b, rb) < 2e-6 and _rms(b, rb) < 1e-6, (relerr(b, rb), _rms(b, rb))
+    plan.close()
