@@ -270,7 +270,9 @@ int finish_out(se2p_plan pl, const OutBuf &o)
 // dir: 0 = D2Z, 1 = Z2D, 2 = R2C (FP32), 3 = C2R (FP32) -- 2D, batch grids;
 // 4 = Z2Z along y (batch contiguous rows of My); 5 = Z2Z along x of one
 // Mx x (My/2+1) half spectrum (stride My/2+1, My/2+1 transforms); 6 = Z2Z
-// along x of transposed half spectra (batch contiguous rows of Mx).
+// along x of transposed half spectra (batch contiguous rows of Mx);
+// 10 + W = R2C of batch grids interleaved per node with stride W (FP32);
+// 20 + W = C2R into grids interleaved with stride W (FP32).
 int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, cufftHandle *h)
 {
     auto key = std::make_tuple(Mx, My, batch, dir);
@@ -303,6 +305,18 @@ int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, c
         int nx = Mx, emb = Mx;
         const int H1 = My / 2 + 1;
         CKF(cufftPlanMany(&p, 1, &nx, &emb, H1, 1, &emb, H1, 1, CUFFT_Z2Z, H1));
+        CKF(cufftSetStream(p, st));
+        pl->ffts[key] = p;
+        *h = p;
+        return SE2P_OK;
+    }
+    if (dir > 10) {
+        const int W = dir % 10, H1 = My / 2 + 1;
+        int re[2] = {Mx, My}, ce[2] = {Mx, H1};
+        if (dir < 20)
+            CKF(cufftPlanMany(&p, 2, n, re, W, 1, ce, 1, cplx_dist, CUFFT_R2C, batch));
+        else
+            CKF(cufftPlanMany(&p, 2, n, ce, 1, cplx_dist, re, W, 1, CUFFT_C2R, batch));
         CKF(cufftSetStream(p, st));
         pl->ffts[key] = p;
         *h = p;
@@ -838,23 +852,30 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         const size_t G = (size_t)Mx * My, H = (size_t)Mx * (My / 2 + 1);
         const int nout = (J.slp ? 2 : 0) + (J.dlp ? 2 : 0);
         const double h = J.Lx / Mx;
+        // grids interleaved per node: the first min(nc, 4) components with
+        // stride W (2 for SLP, 4 otherwise), a fifth one plain after them
+        const int W = nc == 2 ? 2 : 4, nci = std::min(nc, 4), ncp = nc - nci;
         float *grid = nullptr;
         cufftComplex *spec = nullptr;
-        CKS(ensure_t(pl, S_GRID, G * nc, &grid));
+        CKS(ensure_t(pl, S_GRID, G * (size_t)std::max(W + ncp, nout), &grid));
         CKS(ensure_t(pl, S_SPEC, H * nc, &spec));
         CKS(ensure_t(pl, S_UK, ntz * (nout / 2), &uk));
-        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G * nc, ks));
+        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G * (W + ncp), ks));
         SpreadArgsF sa{sp, coef, ns, grid, Mx, My, P, J.Lx / 2.0, J.Ly / 2.0, h, J.w,
                        -2 * J.xi * J.xi / J.eta};
         {
             StageTimer tm(pl, T_SPREAD, ks);
             CK(launch_spread_f32(sa, nc, sm_count(), ks, pl->launches));
         }
-        cufftHandle fwd, inv;
-        CKS(get_fft(pl, ks, Mx, My, nc, 2, &fwd));
+        cufftHandle fwd, fwd1, inv;
+        CKS(get_fft(pl, ks, Mx, My, nci, 10 + W, &fwd));
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
             CKF(cufftExecR2C(fwd, grid, spec));
+            if (ncp) {
+                CKS(get_fft(pl, ks, Mx, My, ncp, 2, &fwd1));
+                CKF(cufftExecR2C(fwd1, grid + (size_t)W * G, spec + (size_t)nci * H));
+            }
         }
         FilterArgsF fa;
         fa.spec = reinterpret_cast<float2 *>(spec);
@@ -873,7 +894,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             StageTimer tm(pl, T_FILTER, ks);
             CK(launch_filter_f32(fa, ks, pl->launches));
         }
-        CKS(get_fft(pl, ks, Mx, My, nout, 3, &inv));
+        CKS(get_fft(pl, ks, Mx, My, nout, 20 + nout, &inv));   // gather reads [node][nout]
         {
             StageTimer tm(pl, T_FFT_INV, ks);
             CKF(cufftExecC2R(inv, spec, grid));

@@ -38,8 +38,11 @@ __device__ __forceinline__ int wrapi(int i, int M)
 }
 
 // ---------------------------------------------------------------------------
-// FP32 spread: one warp per source, lanes over the flattened (P+1)^2 stencil,
-// FP32 atomics into the grids (one per node and component).
+// FP32 spread: one warp per source, lanes over the flattened (P+1)^2 stencil.
+// The grids are interleaved per node ([node][W], W = 2 for the SLP pair, 4
+// otherwise, the DLP-only form's fourth lane zero) so that a node takes one
+// vector atomic (red.global.add.v2/v4.f32) instead of one per component; the
+// fifth component of SLP+DLP follows as a plain grid at grid + 4 G.
 // ---------------------------------------------------------------------------
 constexpr int kSpreadWarpsF = 8;
 
@@ -90,9 +93,16 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
                 const int i = qd / P1, jj = qd - i * P1;
                 const int col = wrapi(smx + i, a.Mx), row = wrapi(smy + jj, a.My);
                 const float wy = wsh[wid][NC][jj];
-                float *g = a.grid + (size_t)col * a.My + row;
-#pragma unroll
-                for (int c = 0; c < NC; c++) atomicAdd(g + c * G, wsh[wid][c][i] * wy);
+                const size_t node = (size_t)col * a.My + row;
+                if (NC == 2) {
+                    atomicAdd(reinterpret_cast<float2 *>(a.grid) + node,
+                              make_float2(wsh[wid][0][i] * wy, wsh[wid][1][i] * wy));
+                } else {
+                    atomicAdd(reinterpret_cast<float4 *>(a.grid) + node,
+                              make_float4(wsh[wid][0][i] * wy, wsh[wid][1][i] * wy,
+                                          wsh[wid][2][i] * wy, NC > 3 ? wsh[wid][3 % NC][i] * wy : 0.f));
+                    if (NC == 5) atomicAdd(a.grid + 4 * G + node, wsh[wid][4 % NC][i] * wy);
+                }
             }
             __syncwarp();
         }
@@ -189,6 +199,8 @@ __global__ void k_filter_f32(FilterArgsF a)
 
 // ---------------------------------------------------------------------------
 // FP32 gather: one lane per target; weights from FP64 exponents, FP32 sums.
+// The NC grids are interleaved per node ([node][NC], the C2R's strided
+// output), one vector load per node.
 // ---------------------------------------------------------------------------
 template <int NC>
 __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
@@ -196,7 +208,6 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nt) return;
     const int P = a.P;
-    const size_t G = (size_t)a.Mx * a.My;
     const double2 T = a.tp[t];
     int mx, my;
     double px, py;
@@ -213,7 +224,7 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
     for (int c = 0; c < NC; c++) acc[c] = 0.f;
     const bool rows_inside = my >= 0 && my + P < a.My;
     for (int i = 0; i <= P; i++) {
-        const float *g = a.grid + (size_t)wrapi(mx + i, a.Mx) * a.My;
+        const size_t col = (size_t)wrapi(mx + i, a.Mx) * a.My;
         float tc[NC];
 #pragma unroll
         for (int c = 0; c < NC; c++) tc[c] = 0.f;
@@ -221,8 +232,20 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
         for (int j = 0; j <= kMaxP; j++) {
             if (j <= P) {
                 const int row = rows_inside ? my + j : wrapi(my + j, a.My);
+                float v[NC];
+                if (NC == 2) {
+                    const float2 q = __ldg(reinterpret_cast<const float2 *>(a.grid) + col + row);
+                    v[0] = q.x;
+                    v[1] = q.y;
+                } else {
+                    const float4 q = __ldg(reinterpret_cast<const float4 *>(a.grid) + col + row);
+                    v[0] = q.x;
+                    v[1 % NC] = q.y;
+                    v[2 % NC] = q.z;
+                    v[3 % NC] = q.w;
+                }
 #pragma unroll
-                for (int c = 0; c < NC; c++) tc[c] = fmaf(wy[j], __ldg(g + c * G + row), tc[c]);
+                for (int c = 0; c < NC; c++) tc[c] = fmaf(wy[j], v[c], tc[c]);
             }
         }
         const float wx = axis_weight(X0, X1, X2, i);
