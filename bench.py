@@ -58,18 +58,25 @@ XI, RC, M, P, L = 860.0, 0.0056, 2688, 24, 1.0
 SEED = 20261203 + 3
 METRIC = "SE Stokes evals/s @1M pts: FP64 tol 1e-10 vs FP32-grid tol 1e-6; fwd+adjoint time"
 UNIT = "evals/s"
-# Roofline inputs of the library's own kernels on this workload.  Algorithmic
-# FP64 work per unit: spread (P+1)^2 (1 + 2 C_in) per source with C_in = 5 grids
-# (SLP f1, f2; DLP S11, S12+S21, S22), gather (P+1)^2 (1 + 2 C_out) per target
-# with C_out = 4.  DRAM bytes per launch are ncu's dram__bytes_read + _write of
-# one launch (profiles/).  The real-space kernel of the FP64 form runs its far
-# pairs in float-float on the FP32 pipe; its bound is instruction issue, so its
-# work is the warp instructions ncu counts per accepted pair evaluation.
+# Roofline inputs of the library's own kernels on this workload (FP64 form).
+# * real space (k_real, far pairs in float-float on the FP32 pipe): bound by
+#   instruction issue; work = warp instructions per accepted pair evaluation
+#   (ncu smsp__inst_executed / evaluations).
+# * spread (k_spread_fix, exact int64 sums): bound by L2 atomics; work = one
+#   64-bit reduction per stencil node and grid, (P+1)^2 C_in per source with
+#   C_in = 5 grids (SLP f1, f2; DLP S11, S12+S21, S22); peak = coalesced int64
+#   atomics measured in this run (torch index_add_).
+# * gather (k_gather_fix, int64 sums of exact products): bound by issue and
+#   load latency; work = warp instructions per target (ncu).
+# * filter: FP64 FLOP against cuBLAS DGEMM.
+# DRAM bytes per launch are ncu's dram__bytes_read + _write of one launch
+# (profiles/).
 C_IN, C_OUT = 5, 4
-SPREAD_FLOP_PER_SOURCE = (P + 1) ** 2 * (1 + 2 * C_IN)
-GATHER_FLOP_PER_TARGET = (P + 1) ** 2 * (1 + 2 * C_OUT)
-DRAM_BYTES = {"spread": 2.832e9, "gather": 0.280e9, "real": 0.243e9}
+SPREAD_RED_PER_SOURCE = (P + 1) ** 2 * C_IN
+FILTER_FLOP_PER_MODE = 60
+DRAM_BYTES = {"spread": 2.008e9, "gather": 0.279e9, "real": 0.267e9}
 REAL_WARP_INST_PER_PAIR = 46.3     # ncu smsp__inst_executed / SLP+DLP pair evaluations
+GATHER_WARP_INST_PER_TARGET = 1508.0   # ncu smsp__inst_executed / targets (k_gather_fix<4,24>)
 
 
 def workload(N):
@@ -228,6 +235,28 @@ def reference_arm(args, rank, world):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def red_peak_gops(torch, dev):
+    """64-bit integer atomic adds to global memory per second, coalesced
+    (consecutive lanes on consecutive words, as the spread's stencil rows),
+    measured with torch's index_add_ over a 64 MB array (best of 5)."""
+    n, m = 2 ** 26, 2 ** 23
+    x = torch.zeros(m, dtype=torch.int64, device=dev)
+    idx = torch.arange(n, device=dev) % m
+    v = torch.ones(n, dtype=torch.int64, device=dev)
+    x.index_add_(0, idx, v)
+    torch.cuda.synchronize(dev)
+    best = 1e30
+    for _ in range(5):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        x.index_add_(0, idx, v)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return n / (best * 1e-3) / 1e9
+
+
 def fp64_peak_tflops(torch, dev):
     """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
     n = 2048
@@ -529,6 +558,10 @@ def gpu_arm(args, rank, world, local_rank):
     legs = set(args.legs.split(","))
     mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev) \
         if "fp32_grid" in legs else None
+    if mixed is not None:
+        # the metric's own pairing: FP32-grid at tolerance 1e-6 against the
+        # FP64 form at tolerance 1e-10 (the headline workload above)
+        mixed["speedup_vs_fp64_tol1e-10"] = mixed["value"] / (1e3 / ms_per_step)
     adjoint = adjoint_leg(plan, args.steps, timed, dev) if "adjoint" in legs else None
     multi = multi_rhs_leg(plan, tens, N, ms_per_step, dev) if "multi_rhs" in legs else None
 
@@ -545,18 +578,26 @@ def gpu_arm(args, rank, world, local_rank):
     evals_per_launch = pairs_per_launch / 2                     # SLP and DLP share each evaluation
     clock_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_peak = 4 * sms * clock_ghz * 1e9 / 1e12
+    issue_src = "4 warp instructions per clock per SM x SMs x measured SM clock"
     if top == "real":
         achieved = evals_per_launch * REAL_WARP_INST_PER_PAIR / (top_ms * 1e-3) / 1e12
         roof = {"kernel": "k_real<SLP,DLP,float-float> (fused real-space pair sum)",
-                "bound": "issue", "achieved": achieved,
-                "peak": 4 * sms * clock_ghz * 1e9 / 1e12, "unit": "T warp-inst/s",
-                "peak_source": "4 warp instructions per clock per SM x SMs x measured SM clock"}
+                "bound": "issue", "achieved": achieved, "peak": issue_peak,
+                "unit": "T warp-inst/s", "peak_source": issue_src}
+    elif top == "gather":
+        roof = {"kernel": "k_gather_fix<4,24> (integer gather, 4 grids)", "bound": "issue",
+                "achieved": N * GATHER_WARP_INST_PER_TARGET / (top_ms * 1e-3) / 1e12,
+                "peak": issue_peak, "unit": "T warp-inst/s", "peak_source": issue_src}
+    elif top == "spread":
+        roof = {"kernel": "k_spread_fix<5> (integer spread, 5 grids)", "bound": "l2_atomics",
+                "achieved": N * SPREAD_RED_PER_SOURCE / (top_ms * 1e-3) / 1e9,
+                "peak": red_peak_gops(torch, dev), "unit": "G int64 atomics/s",
+                "peak_source": "coalesced int64 index_add_ measured in this run "
+                               "(MEASURED_PEAKS.json holds no atomic figure)"}
     else:
-        flops = (N * SPREAD_FLOP_PER_SOURCE if top == "spread" else N * GATHER_FLOP_PER_TARGET)
-        roof = {"kernel": {"spread": "k_spread<5> (Gaussian spread, 5 grids)",
-                           "gather": "k_gather<4,24> (Gaussian gather, 4 grids)",
-                           "filter": "k_filter"}[top],
-                "bound": "fp64", "achieved": flops / (top_ms * 1e-3) / 1e12,
+        flops = M * (M // 2 + 1) * FILTER_FLOP_PER_MODE
+        roof = {"kernel": "k_filter", "bound": "fp64", "achieved": flops / (top_ms * 1e-3) / 1e12,
                 "peak": fp64_peak_tflops(torch, dev), "unit": "TFLOP/s",
                 "peak_source": "cuBLAS DGEMM 2048^3 measured in this run "
                                "(MEASURED_PEAKS.json holds no FP64 figure)"}
