@@ -45,6 +45,7 @@ enum Slot {
     S_GCOEF, S_GCOEFF, S_GUR0, S_GUR1,          // geometry apply scratch
     S_SBINS, S_GMAX,                            // fixed-point spread bound, gather scale
     S_TWY, S_TWX,                               // float-float FFT twiddles (y, x lengths)
+    S_SPL, S_TPL,                               // low halves of sorted positions (FP32 grid)
     S_COUNT_SLOTS
 };
 
@@ -739,17 +740,22 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     CKS(ensure_t(pl, S_SP, nsz, &sp));
     CKS(ensure_t(pl, S_TP, ntz, &tp));
 
-    float2 *spf = nullptr, *tpf = nullptr;
+    float2 *spf = nullptr, *tpf = nullptr, *spl = nullptr, *tpl = nullptr;
+    const bool f32 = pl->precision == SE2P_PRECISION_FP32_GRID;
     if (J.real) {
         CKS(ensure_t(pl, S_SPF, nsz, &spf));
         CKS(ensure_t(pl, S_TPF, ntz, &tpf));
+        if (f32) {
+            CKS(ensure_t(pl, S_SPL, nsz, &spl));
+            CKS(ensure_t(pl, S_TPL, ntz, &tpl));
+        }
     }
     {
     StageTimer tm(pl, T_SORT);
     BinArgs bs{ws, ns, J.Lx, J.Ly, nx, ny, sbox, srank, count};
-    CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, spf, st, pl->launches));
+    CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, spf, st, pl->launches, spl));
     BinArgs bt{wt, nt, J.Lx, J.Ly, nx, ny, tbox, trank, count};
-    CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, tpf, st, pl->launches));
+    CK(launch_bin(bt, tstart, nbox, tperm, tboxs, tp, tpf, st, pl->launches, tpl));
     }
 
     const int nc = (J.slp ? 2 : 0) + (J.dlp ? 3 : 0);
@@ -813,11 +819,14 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ra.ncf = 0;
         ra.doff_ff = 0;
         ra.gtab = nullptr;
-        if (form == kFormFF) {
+        ra.spl = spl;
+        ra.tpl = tpl;
+        if (form == kFormFF || form == kFormF32) {
+            // float-float coefficients (the FP32-grid form reads their high halves)
             const int ncf = (J.slp ? 2 : 0) + (J.dlp ? 5 : 0);
             float2 *cff = nullptr;
             CKS(ensure_t(pl, S_COEF_FF, (size_t)ncf * nsz, &cff));
-            CKS(gtab_device(pl, st, &ra.gtab));
+            if (form == kFormFF) CKS(gtab_device(pl, st, &ra.gtab));
             StageTimer tm(pl, T_COEF);
             CK(launch_src_coef_ff(ns, coef, nc, J.slp, J.dlp, cff, ncf, st, pl->launches));
             ra.coef_ff = cff;

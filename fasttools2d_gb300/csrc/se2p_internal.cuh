@@ -266,6 +266,10 @@ struct RealArgs {
     // the piecewise fit of the E1 Pade form (kGPieces x 3 float4)
     const float2 *coef_ff;
     int ncf, doff_ff;
+    // FP32-grid form only: the low halves of the sorted positions (spf, tpf
+    // being the high halves of float-float pairs), so that far-pair offsets
+    // are formed exactly on the FP32 pipe
+    const float2 *spl = nullptr, *tpl = nullptr;
     const float4 *gtab;
     // adjoint only: outer points are the forward sources (sp/spf/coef, boxes
     // obox), inner candidates the forward targets (cell list sstart, tp/tpf,
@@ -359,7 +363,8 @@ struct GatherArgsF {
 // ---------------------------------------------------------------------------
 cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *sorted_box,
                        double2 *sorted_pos, float2 *sorted_pos_f, cudaStream_t st,
-                       int64_t &launches);
+                       int64_t &launches,
+                       float2 *sorted_pos_lo = nullptr);
 cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
                             const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
                             cudaStream_t st, int64_t &launches);

@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, in
 __global__ void k_bin_place(int64_t n, const int *__restrict__ box, const int *__restrict__ rank,
                             const int *__restrict__ start, int *__restrict__ perm,
                             int *__restrict__ sorted_box, const double2 *__restrict__ p,
-                            double2 *__restrict__ sp, float2 *__restrict__ spf)
+                            double2 *__restrict__ sp, float2 *__restrict__ spf,
+                            float2 *__restrict__ spl)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -92,7 +93,11 @@ __global__ void k_bin_place(int64_t n, const int *__restrict__ box, const int *_
     if (sorted_box) sorted_box[j] = b;
     const double2 q = p[i];
     sp[j] = q;
-    if (spf) spf[j] = make_float2((float)q.x, (float)q.y);
+    const float hx = (float)q.x, hy = (float)q.y;
+    if (spf) spf[j] = make_float2(hx, hy);
+    // q - hi is exact in FP64; its rounding to FP32 leaves hi + lo within
+    // 2^-48 |q| of q
+    if (spl) spl[j] = make_float2((float)(q.x - (double)hx), (float)(q.y - (double)hy));
 }
 
 // Per-source coefficients in sorted order, nc per source: SLP f (f1, f2),
@@ -249,6 +254,8 @@ struct RealWarp {
     int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
     double2 nbz[9];
     float2 nbzf[9];
+    // FP32-grid form: target position as float-float (hi.x, hi.y, lo.x, lo.y)
+    float4 tposff[kRing];
 };
 
 // Segmented warp reduction of (v0..v3) by nondecreasing key; the last lane
@@ -397,22 +404,29 @@ __constant__ float c_e1f[3][22] = {
 // FP64 in each kernel's own order, then everything runs in FP32.
 template <bool SLP, bool DLP>
 __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp &W, int2 e,
-                                              const float *e1f, float &s1, float &s2, float &d1,
+                                              const float *e1f, const float4 &zxf,
+                                              const float4 &zyf, float &s1, float &s2, float &d1,
                                               float &d2)
 {
     const int s = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
-    const double2 S = a.sp[s];
-    const double2 T = W.tpos[slot];
     const int tb = W.tbox[slot];
     const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
-    // one FP64 offset (a second add only across a periodic image), rounded to
-    // FP32 through the bit-pattern split (conversions run at the FP64 rate)
-    double dx = S.x - T.x, dy = S.y - T.y;
-    if (ux < 0 || ux >= a.nx || uy < 0 || uy >= a.ny) {
-        dx += ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-        dy += uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
-    }
-    const float x1 = ff_split(dx).x, x2 = ff_split(dy).x;
+    // The offset s - t + z from float-float positions, on the FP32 pipe: the
+    // TwoSum of the high halves is exact, the image shift z (zxf = (z-.hi,
+    // z-.lo, z+.hi, z+.lo)) cancels its head exactly (Sterbenz: the two are
+    // within a factor of 2 across a periodic image), and the low-order terms
+    // follow; one rounding to FP32 at the end.
+    const float2 Sh = a.spf[s], Sl = a.spl[s];
+    const float4 Tq = W.tposff[slot];
+    const float2 zx = ux < 0 ? make_float2(zxf.x, zxf.y)
+                             : (ux >= a.nx ? make_float2(zxf.z, zxf.w) : make_float2(0.f, 0.f));
+    const float2 zy = uy < 0 ? make_float2(zyf.x, zyf.y)
+                             : (uy >= a.ny ? make_float2(zyf.z, zyf.w) : make_float2(0.f, 0.f));
+    float px, ex, py, ey;
+    two_sum(Sh.x, -Tq.x, px, ex);
+    two_sum(Sh.y, -Tq.y, py, ey);
+    const float x1 = (px + zx.x) + ((ex + (Sl.x - Tq.z)) + zx.y);
+    const float x2 = (py + zy.x) + ((ey + (Sl.y - Tq.w)) + zy.y);
     const float dxs = x1, dys = x2;
     const float xi2 = a.xi2f;
     if (SLP && (fl & 1)) {
@@ -431,22 +445,24 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
         }
         const float E = set == 2 ? __fdividef(pa, pb) + x - __logf(x) - 0.66373538970947265625f
                                  : ex * (z + __fdividef(pa, pb + x));
-        const float f1 = (float)a.coef[(int64_t)a.nc * s], f2 = (float)a.coef[(int64_t)a.nc * s + 1];
+        // coefficients: the high halves of the float-float copy (no FP64-rate conversion)
+        const float f1 = a.coef_ff[(int64_t)a.ncf * s].x, f2 = a.coef_ff[(int64_t)a.ncf * s + 1].x;
         const float h = 0.5f * E, gq = ex * ir2 * fmaf(dxs, f2, -dys * f1);
         s1 = fmaf(h, f1, fmaf(gq, dys, s1));
         s2 = fmaf(h, f2, fmaf(-gq, dxs, s2));
     }
     if (DLP && (fl & 2)) {
-        const double *Sc = a.coef + (int64_t)a.nc * s + a.doff;
-        const float S11 = (float)Sc[0], S1221 = (float)Sc[1], S22 = (float)Sc[2];
+        const float2 *Sc = a.coef_ff + (int64_t)a.ncf * s + a.doff_ff;
+        const float S11 = Sc[0].x, S1221 = Sc[1].x, S22 = Sc[2].x;
+        const float T1 = Sc[3].x, T2 = Sc[4].x;   // 3 S11 + S22, 3 S22 + S11
         const float r2 = fmaf(x1, x1, x2 * x2);
         const float x = r2 * xi2;
         const float ex = __expf(-x);
         const float ir2 = __frcp_rn(r2);
         const float fb = -4.f * (1.f + x) * ir2 * ir2;
         const float Q = fmaf(x1 * x1, S11, fmaf(x1 * x2, S1221, x2 * x2 * S22));
-        const float A1 = fmaf(x1, fmaf(3.f, S11, S22), x2 * S1221);
-        const float A2 = fmaf(x2, fmaf(3.f, S22, S11), x1 * S1221);
+        const float A1 = fmaf(x1, T1, x2 * S1221);
+        const float A2 = fmaf(x2, T2, x1 * S1221);
         const float fq = fb * Q, pf = 2.f * xi2;
         d1 = fmaf(ex, fmaf(fq, x1, pf * A1), d1);
         d2 = fmaf(ex, fmaf(fq, x2, pf * A2), d2);
@@ -526,6 +542,11 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
         tabff[i] = ff_split(c_exp_tab[i]);
     }
     const float2 xi2ff = ff_split(a.xi2), pfff = ff_split(a.pf);
+    // image shifts as float-float, for the FP32-grid form's offsets
+    const float2 zmx = ff_split(a.zxm), zpx = ff_split(a.zxp);
+    const float2 zmy = ff_split(a.zym), zpy = ff_split(a.zyp);
+    const float4 zxf = make_float4(zmx.x, zmx.y, zpx.x, zpx.y);
+    const float4 zyf = make_float4(zmy.x, zmy.y, zpy.x, zpy.y);
     // Queue 0 (the fast pairs): float-float pairs 1 < x < 64 with margins
     // for the FP32 pre-test; FP32-grid form, x > 1 (near pairs, E1 at small
     // argument, stay FP64 in both forms).
@@ -584,7 +605,7 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
             }
         }
         if (lane < cnt) {
-            if (f32) real_pair_f32<SLP, DLP>(a, W, e, e1f, P.f1, P.f2, P.g1, P.g2);
+            if (f32) real_pair_f32<SLP, DLP>(a, W, e, e1f, zxf, zyf, P.f1, P.f2, P.g1, P.g2);
             else if (ffp)
                 real_pair_ff<SLP, DLP>(a, W, e, tabff, xi2ff, pfff, P.h1, P.h2, P.k1, P.k2);
             else real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
@@ -643,6 +664,10 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
             W.tpos[slot] = T;
             W.tbox[slot] = tb;
             W.tidx[slot] = t;
+            if (MIXED) {
+                const float2 tl = a.tpl[t];
+                W.tposff[slot] = make_float4(Tf.x, Tf.y, tl.x, tl.y);
+            }
         }
         // neighbour boxes: first source, counts -> list prefix, image shift
         int cntk = 0;
@@ -2465,7 +2490,7 @@ int sm_count()
 
 cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *sorted_box,
                        double2 *sorted_pos, float2 *sorted_pos_f, cudaStream_t st,
-                       int64_t &launches)
+                       int64_t &launches, float2 *sorted_pos_lo)
 {
     cudaError_t e = cudaMemsetAsync(a.count, 0, sizeof(int) * (size_t)nbox, st);
     if (e != cudaSuccess) return e;
@@ -2478,7 +2503,7 @@ cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *s
     if (a.n > 0) {
         k_bin_place<<<grid_for(a.n, 256), 256, 0, st>>>(a.n, a.box, a.rank, start, perm,
                                                          sorted_box, a.p, sorted_pos,
-                                                         sorted_pos_f);
+                                                         sorted_pos_f, sorted_pos_lo);
         launches++;
     }
     return cudaGetLastError();
