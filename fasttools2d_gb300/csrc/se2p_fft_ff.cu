@@ -190,7 +190,8 @@ template <>
 __device__ __forceinline__ void dft<7>(fc *v, float s, const fc *cst) { dft_odd<7>(v, s, cst); }
 
 template <int R>
-__device__ void stage(const float *A, float *B, int L, int Ns, float s, const float4 *tw)
+__device__ void stage(const float *A, float *B, int L, int Ns, unsigned magic, float s,
+                      const float4 *tw)
 {
     // the constants of the R-point DFT from the twiddle table
     fc cst[R / 2 > 0 ? R / 2 : 1];
@@ -206,7 +207,7 @@ __device__ void stage(const float *A, float *B, int L, int Ns, float s, const fl
     }
     const int nb = L / R, stride = L / (Ns * R), Lp = sh_len(L);
     for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-        const int k = j % Ns;
+        const int k = Ns == 1 ? 0 : j - (int)__umulhi((unsigned)j, magic) * Ns;   // j mod Ns
         fc v[R];
 #pragma unroll
         for (int r = 0; r < R; r++) v[r] = sh_get(A, Lp, j + r * nb);
@@ -304,13 +305,14 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
         int Ns = 1;
         for (int st = 0; st < p.nst; st++) {
             const int R = p.radix[st];
+            const unsigned mg = p.magic[st];
             switch (R) {
-            case 8: stage<8>(A, B, L, Ns, s, tw); break;
-            case 4: stage<4>(A, B, L, Ns, s, tw); break;
-            case 2: stage<2>(A, B, L, Ns, s, tw); break;
-            case 7: stage<7>(A, B, L, Ns, s, tw); break;
-            case 5: stage<5>(A, B, L, Ns, s, tw); break;
-            default: stage<3>(A, B, L, Ns, s, tw); break;
+            case 8: stage<8>(A, B, L, Ns, mg, s, tw); break;
+            case 4: stage<4>(A, B, L, Ns, mg, s, tw); break;
+            case 2: stage<2>(A, B, L, Ns, mg, s, tw); break;
+            case 7: stage<7>(A, B, L, Ns, mg, s, tw); break;
+            case 5: stage<5>(A, B, L, Ns, mg, s, tw); break;
+            default: stage<3>(A, B, L, Ns, mg, s, tw); break;
             }
             Ns *= R;
             float *t = A;
@@ -343,6 +345,12 @@ bool fft_rows_ff_plan(int L, FftRowsFF &p)
     while (n % 2 == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = 2; n /= 2; }
     for (int r : {7, 5, 3})
         while (n % r == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = r; n /= r; }
+    unsigned long long Ns = 1;
+    for (int st = 0; st < p.nst; st++) {
+        // (the first stage, Ns = 1, takes k = 0 without it)
+        p.magic[st] = Ns == 1 ? 0u : (unsigned)(((1ull << 32) + Ns - 1) / Ns);
+        Ns *= (unsigned long long)p.radix[st];
+    }
     return n == 1;
 }
 

@@ -398,6 +398,9 @@ constexpr int kFftFFMaxStages = 16;
 struct FftRowsFF {
     int L = 0, nst = 0, sign = -1;
     int radix[kFftFFMaxStages] = {};
+    // ceil(2^32 / Ns) of each stage (Ns = product of the earlier radices):
+    // j / Ns = umulhi(j, magic) exactly for j Ns < 2^32
+    unsigned magic[kFftFFMaxStages] = {};
 };
 bool fft_rows_ff_plan(int L, FftRowsFF &p);
 void fft_rows_ff_twiddles(int L, float4 *host);   // exp(-2 pi i m/L), m < L, float-float
