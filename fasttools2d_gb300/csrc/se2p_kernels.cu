@@ -527,7 +527,7 @@ struct PairQueue {
 };
 
 template <bool SLP, bool DLP, int FORM>
-__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealArgs a)
+__global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
 {
     constexpr bool MIXED = FORM == kFormF32;
     constexpr bool FF = FORM == kFormFF;
@@ -2541,11 +2541,12 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
 {
     if (a.ntar <= 0) return cudaSuccess;
     const int64_t want = (a.ntar + kRealWarps - 1) / kRealWarps;
-    // Five 4-warp blocks per SM (94 registers: 20 warps resident), persistent
-    // over the sorted targets.  The k-space chain (high-priority stream) takes
-    // what is left; with 8-warp blocks only 16 warps fitted and the
-    // evaluation took 19.9 instead of 18.6 ms at 2^20 points.
-    const int64_t cap = (int64_t)sm_count() * 5;
+    // Six 4-warp blocks per SM (the launch bound holds 80 registers: 24 warps
+    // resident), persistent over the sorted targets.  The k-space chain
+    // (high-priority stream) takes what is left.  With 8-warp blocks at 94
+    // registers only 16 warps fitted: 19.9 ms per evaluation at 2^20 points,
+    // against 18.6 with 20 warps and 18.45 with 24.
+    const int64_t cap = (int64_t)sm_count() * 6;
     const unsigned g = (unsigned)(want < cap ? want : cap);
     if (form == kFormF32) launch_real_form<kFormF32>(a, slp, dlp, g, st);
     else if (form == kFormFF) launch_real_form<kFormFF>(a, slp, dlp, g, st);
