@@ -46,6 +46,7 @@ enum Slot {
     S_SBINS, S_GMAX,                            // fixed-point spread bound, gather scale
     S_TWY, S_TWX,                               // float-float FFT twiddles (y, x lengths)
     S_SPL, S_TPL,                               // low halves of sorted positions (FP32 grid)
+    S_MTAB,                                     // cached per-mode filter multipliers
     S_COUNT_SLOTS
 };
 
@@ -81,6 +82,7 @@ struct se2p_plan_st {
     bool timing = false;
     bool count_pairs = false;
     double ftab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // (Mx, My, Lx, Ly, xi, eta, layout) of S_FTAB
+    double mtab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // the same for S_MTAB
     bool gtab_ready = false;                   // S_GTAB holds the E1 fit
     // float-float FFT twiddles: the length and device copy each slot holds,
     // and the host tables the (asynchronous) uploads read from
@@ -352,6 +354,27 @@ int filter_table(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
         memcpy(pl->ftab_key, key, sizeof key);
     }
     fa.etab = tab;
+    return SE2P_OK;
+}
+
+// The forward filter's effective per-mode multipliers (k_filter_matrix_table),
+// kept like the factor table; k_filter then does two small complex mat-vecs
+// per mode (20 FP64 operations instead of about 60).
+int filter_matrix(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
+{
+    const double key[7] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta,
+                           (double)fa.transposed};
+    const size_t H = (size_t)fa.Mx * (fa.My / 2 + 1);
+    const bool have = pl->buf[S_MTAB].p &&
+                      pl->buf[S_MTAB].bytes >= H * kFilterMat * sizeof(double) &&
+                      memcmp(key, pl->mtab_key, sizeof key) == 0;
+    double *tab = nullptr;
+    CKS(ensure_t(pl, S_MTAB, H * kFilterMat, &tab));
+    if (!have) {
+        CK(launch_filter_matrix_table(fa, tab, st, pl->launches));
+        memcpy(pl->mtab_key, key, sizeof key);
+    }
+    fa.mtab = tab;
     return SE2P_OK;
 }
 
@@ -981,7 +1004,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.transposed = 1;
         {
             StageTimer tm(pl, T_FILTER, ks);
-            CKS(filter_table(pl, fa, ks));
+            CKS(filter_matrix(pl, fa, ks));
             CK(launch_filter(fa, ks, pl->launches));
         }
 

@@ -314,7 +314,14 @@ struct FilterArgs {
     int slp_out, dlp_out;       // where the 2 filtered spectra of each kind go
     const double2 *etab;        // per-mode (SLP e, DLP e*t) from k_filter_table, or NULL
     int transposed = 0;         // spectra stored [c][ky][x] (x fastest) instead of [c][x][ky]
+    // per-mode effective multipliers from k_filter_matrix_table (forward
+    // filter only), or NULL: kFilterMat doubles per mode
+    const double *mtab = nullptr;
 };
+// SLP (a, b, c): o1 = a h1 - b h2, o2 = -b h1 + c h2; DLP rows (B111, B112,
+// B122) and (B211, B212, B222) times e t; Nyquist averaging, zero mode and
+// 1/(Mx My) folded in.
+constexpr int kFilterMat = 9;
 
 struct GatherArgs {
     const double2 *tp;
@@ -460,6 +467,8 @@ cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
                                 int64_t &launches);
+cudaError_t launch_filter_matrix_table(const FilterArgs &a, double *mtab, cudaStream_t st,
+                                       int64_t &launches);
 cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches);
 cudaError_t launch_wrap(int64_t n, const double2 *p, double Lx, double Ly, double2 *out,
                         cudaStream_t st, int64_t &launches);

@@ -1830,6 +1830,28 @@ __global__ void k_filter(FilterArgs a)
         jy = (int)(idx - (int64_t)jx * H);
     }
     double2 *sp = reinterpret_cast<double2 *>(a.spec);
+    if (a.mtab) {
+        // the cached effective multipliers (k_filter_matrix_table)
+        const double *m = a.mtab + (int64_t)kFilterMat * idx;
+        if (a.slp_in >= 0) {
+            const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
+            const double ma = m[0], mb = m[1], mc = m[2];
+            sp[a.slp_out * G + idx] = make_double2(fma(ma, h1.x, -mb * h2.x), fma(ma, h1.y, -mb * h2.y));
+            sp[(a.slp_out + 1) * G + idx] =
+                make_double2(fma(mc, h2.x, -mb * h1.x), fma(mc, h2.y, -mb * h1.y));
+        }
+        if (a.dlp_in >= 0) {
+            const double2 h1 = sp[a.dlp_in * G + idx], h23 = sp[(a.dlp_in + 1) * G + idx];
+            const double2 h4 = sp[(a.dlp_in + 2) * G + idx];
+            const double2 t1 = make_double2(fma(m[3], h1.x, fma(m[4], h23.x, m[5] * h4.x)),
+                                            fma(m[3], h1.y, fma(m[4], h23.y, m[5] * h4.y)));
+            const double2 t2 = make_double2(fma(m[6], h1.x, fma(m[7], h23.x, m[8] * h4.x)),
+                                            fma(m[6], h1.y, fma(m[7], h23.y, m[8] * h4.y)));
+            sp[a.dlp_out * G + idx] = make_double2(t1.y, -t1.x);            // -i
+            sp[(a.dlp_out + 1) * G + idx] = make_double2(t2.y, -t2.x);
+        }
+        return;
+    }
     const bool zero = (jx == 0 && jy == 0);
     const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
     const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
@@ -1901,6 +1923,60 @@ __global__ void k_filter_table(FilterArgs a, double2 *tab)
         return;
     }
     tab[idx] = make_double2(slp_factor(K2, a.xi, a.eta), dlp_factor(K2, a.xi, a.eta));
+}
+
+// Per-mode effective multipliers of k_filter (its arithmetic, once per
+// parameter set): the SLP matrix e [[k2^2, -k1 k2], [-k1 k2, k1^2]] and the
+// DLP rows e t (B1., B2.), averaged with the index partner on the Nyquist
+// lines (even for the SLP, odd for the DLP), times 1/(Mx My); zero at k = 0.
+__global__ void k_filter_matrix_table(FilterArgs a, double *__restrict__ mtab)
+{
+    const int H = a.My / 2 + 1;
+    const int64_t G = (int64_t)a.Mx * H;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G) return;
+    int jx, jy;
+    if (a.transposed) {
+        jy = (int)(idx / a.Mx);
+        jx = (int)(idx - (int64_t)jy * a.Mx);
+    } else {
+        jx = (int)(idx / H);
+        jy = (int)(idx - (int64_t)jx * H);
+    }
+    double *m = mtab + (int64_t)kFilterMat * idx;
+    if (jx == 0 && jy == 0) {
+        for (int i = 0; i < kFilterMat; i++) m[i] = 0.0;
+        return;
+    }
+    const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
+    const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
+    const double k1p = (jx == a.Mx / 2) ? k1 : -k1;
+    const double k2p = (jy == a.My / 2) ? k2 : -k2;
+    const double K2 = k1 * k1 + k2 * k2;
+    const double sc = a.scale;
+    const double e = slp_factor(K2, a.xi, a.eta), et = dlp_factor(K2, a.xi, a.eta);
+    // SLP
+    double b = k1 * k2;
+    if (nyq) b = 0.5 * (b + k1p * k2p);
+    m[0] = k2 * k2 * e * sc;
+    m[1] = b * e * sc;
+    m[2] = k1 * k1 * e * sc;
+    // DLP (mex_stokes_dlp_kspace.cpp:228-251)
+    double B[6], Bp[6];
+    auto bmat = [](double q1, double q2, double Q2, double *o) {
+        o[0] = 3.0 * q1 * Q2 - 2.0 * q1 * q1 * q1;
+        o[1] = q2 * Q2 - 2.0 * q1 * q1 * q2;
+        o[2] = q1 * Q2 - 2.0 * q1 * q2 * q2;
+        o[3] = q2 * Q2 - 2.0 * q2 * q1 * q1;
+        o[4] = q1 * Q2 - 2.0 * q2 * q1 * q2;
+        o[5] = 3.0 * q2 * Q2 - 2.0 * q2 * q2 * q2;
+    };
+    bmat(k1, k2, K2, B);
+    if (nyq) {
+        bmat(k1p, k2p, K2, Bp);
+        for (int i = 0; i < 6; i++) B[i] = 0.5 * (B[i] - Bp[i]);
+    }
+    for (int i = 0; i < 6; i++) m[3 + i] = et * B[i] * sc;
 }
 
 // ===========================================================================
@@ -2577,6 +2653,15 @@ cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t 
 {
     const int64_t n = (int64_t)a.Mx * (a.My / 2 + 1);
     k_filter_table<<<grid_for(n, 256), 256, 0, st>>>(a, tab);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter_matrix_table(const FilterArgs &a, double *mtab, cudaStream_t st,
+                                       int64_t &launches)
+{
+    const int64_t n = (int64_t)a.Mx * (a.My / 2 + 1);
+    k_filter_matrix_table<<<grid_for(n, 256), 256, 0, st>>>(a, mtab);
     launches++;
     return cudaGetLastError();
 }
