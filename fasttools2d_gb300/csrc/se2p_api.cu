@@ -639,10 +639,11 @@ static bool fft_ff_ok(int Mx, int My)
 
 // One batch of 1D row transforms: cuFFT plan `dir` or the float-float rows.
 static int fft_rows(se2p_plan pl, cudaStream_t ks, bool ff, int Mx, int My, int L, int64_t rows,
-                    int dir, double2 *data, int sign)
+                    int dir, double2 *data, int sign, const FftRowsFF *io = nullptr)
 {
     if (ff) {
         FftRowsFF p;
+        if (io) p = *io;                             // fused pack / unpack fields
         fft_rows_ff_plan(L, p);
         p.sign = sign;
         const float4 *tw = nullptr;
@@ -668,12 +669,23 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
     const int H1 = My / 2 + 1, ncg = (nc + 1) / 2;
     const size_t G = (size_t)Mx * My;
     double2 *zgd = reinterpret_cast<double2 *>(zg);
-    if (fixb)
-        CK(launch_pack_fixed_pairs(reinterpret_cast<const long long *>(grid), nc, (int64_t)G, fixb,
-                                   zgd, ks, pl->launches));
-    else
-        CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
-    CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1));
+    if (ff) {
+        // the pack is fused into the float-float y pass
+        FftRowsFF io;
+        io.Mx = Mx;
+        io.G = (int64_t)G;
+        io.pack_in = grid;
+        io.bound = fixb;
+        io.npl_in = nc;
+        CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1, &io));
+    } else {
+        if (fixb)
+            CK(launch_pack_fixed_pairs(reinterpret_cast<const long long *>(grid), nc, (int64_t)G,
+                                       fixb, zgd, ks, pl->launches));
+        else
+            CK(launch_pack_real_pairs(grid, nc, (int64_t)G, zgd, ks, pl->launches));
+        CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1));
+    }
     CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
                                    pl->launches));
     CKS(fft_rows(pl, ks, ff, Mx, My, Mx, (int64_t)nc * H1, 6, reinterpret_cast<double2 *>(spec), -1));
@@ -692,8 +704,19 @@ static int fft_inv_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, cufftDouble
     CKS(fft_rows(pl, ks, ff, Mx, My, Mx, (int64_t)nout * H1, 6, reinterpret_cast<double2 *>(spec), 1));
     CK(launch_join_half_spectra_t(reinterpret_cast<double2 *>(spec), nout, Mx, My, zgd, ks,
                                   pl->launches));
-    CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)npo * Mx, 4, zgd, 1));
-    CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches, gmax));
+    if (ff) {
+        // the unpack (and the grid maximum) is fused into the float-float y pass
+        FftRowsFF io;
+        io.Mx = Mx;
+        io.G = (int64_t)G;
+        io.unpack_out = grid;
+        io.npl_out = nout;
+        io.gmax = gmax;
+        CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)npo * Mx, 4, zgd, 1, &io));
+    } else {
+        CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)npo * Mx, 4, zgd, 1));
+        CK(launch_unpack_real_pairs(zgd, nout, (int64_t)G, grid, ks, pl->launches, gmax));
+    }
     return SE2P_OK;
 }
 

@@ -255,6 +255,42 @@ __device__ __forceinline__ double ff_to_double_scaled(float hi, float lo, int e)
     return __longlong_as_double((long long)bits);
 }
 
+// a > 0 rounded to 24 bits (to nearest, ties up): the float's bit pattern,
+// and in *rem the remainder a - rounded (|rem| <= 2^(bits-25)).  a < 2^62.
+__device__ __forceinline__ unsigned u64_round_float(unsigned long long a, long long *rem)
+{
+    const int nb = 64 - __clzll(a);
+    const int sh = nb - 24;
+    unsigned long long mh;
+    if (sh <= 0) {
+        mh = a << (-sh);
+        if (rem) *rem = 0;
+    } else {
+        mh = (a + (1ull << (sh - 1))) >> sh;
+        if (rem) *rem = (long long)a - (long long)(mh << sh);
+    }
+    int ex = nb - 1;
+    if (mh >> 24) {                                  // rounding carried into bit 24
+        mh >>= 1;
+        ex++;
+    }
+    return ((unsigned)(ex + 127) << 23) | ((unsigned)mh & 0x7fffffu);
+}
+
+// An int64 (|v| < 2^62) as float-float with integer operations.
+__device__ __forceinline__ float2 ll_to_ff(long long v)
+{
+    if (v == 0) return make_float2(0.f, 0.f);
+    const unsigned sv = v < 0 ? 0x80000000u : 0u;
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    long long r;
+    const float hi = __uint_as_float(sv | u64_round_float(a, &r));
+    if (r == 0) return make_float2(hi, 0.f);
+    const unsigned sr = ((r < 0) != (v < 0)) ? 0x80000000u : 0u;
+    const unsigned long long ar = r < 0 ? 0ull - (unsigned long long)r : (unsigned long long)r;
+    return make_float2(hi, __uint_as_float(sr | u64_round_float(ar, nullptr)));
+}
+
 // d 2^-e as float-float (ff_split of the scaled value, the scaling done on
 // the exponent field)
 __device__ __forceinline__ float2 ff_split_scaled(double d, int e)
@@ -277,29 +313,54 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
     const int L = p.L, Lp = sh_len(L);
     const float s = (float)p.sign;
     float *A = fsh, *B = fsh + 4 * Lp;
+    // fused pack from int64 planes: the values need no row scaling (|v| <
+    // 2^60 stays far inside the float range after the transform's growth by
+    // at most L); the 2^-S of the fixed-point grid is applied on the way out
+    const unsigned long long bnd = p.bound ? *p.bound : kFixedOff;
+    const bool fixed_in = p.pack_in && bnd != kFixedOff;
+    const int S = fixed_in ? fix_shift(bnd) : 0;
     for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
         double2 *d = data + row * L;
-        // the row as doubles into B (4 Lp floats >= L double2), and its
-        // largest exponent
-        double2 *raw = reinterpret_cast<double2 *>(B);
-        int em = 0;
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const double2 v = d[k];
-            raw[k] = v;
-            em = max(em, max((__double2hiint(v.x) >> 20) & 0x7ff, (__double2hiint(v.y) >> 20) & 0x7ff));
-        }
-        for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(~0u, em, o));
-        if ((threadIdx.x & 31) == 0) emax_w[threadIdx.x >> 5] = em;
-        __syncthreads();
-        em = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) em = max(em, emax_w[w]);
-        // scale 2^-e brings the largest finite entry to [2^63, 2^64) (no
-        // scaling of a zero row or of one with an inf or NaN, which then
-        // spreads through the row as in an FP64 transform)
-        const int e = (em == 0 || em == 0x7ff) ? 0 : em - 1023 - 63;
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const double2 v = raw[k];
-            sh_put(A, Lp, k, fc{ff_split_scaled(v.x, e), ff_split_scaled(v.y, e)});
+        const int64_t q = p.Mx ? row / p.Mx : 0, xr = row - q * p.Mx;
+        const int64_t off_re = (2 * q) * p.G + xr * L, off_im = (2 * q + 1) * p.G + xr * L;
+        int e;
+        if (fixed_in) {
+            const long long *g = static_cast<const long long *>(p.pack_in);
+            const bool has_im = 2 * q + 1 < p.npl_in;
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const long long vr = g[off_re + k], vi = has_im ? g[off_im + k] : 0;
+                sh_put(A, Lp, k, fc{ll_to_ff(vr), ll_to_ff(vi)});
+            }
+            e = -S;
+        } else {
+            // the row as doubles into B (4 Lp floats >= L double2), and its
+            // largest exponent
+            double2 *raw = reinterpret_cast<double2 *>(B);
+            int em = 0;
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                double2 v;
+                if (p.pack_in) {
+                    const double *g = static_cast<const double *>(p.pack_in);
+                    v = make_double2(g[off_re + k], 2 * q + 1 < p.npl_in ? g[off_im + k] : 0.0);
+                } else {
+                    v = d[k];
+                }
+                raw[k] = v;
+                em = max(em, max((__double2hiint(v.x) >> 20) & 0x7ff, (__double2hiint(v.y) >> 20) & 0x7ff));
+            }
+            for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(~0u, em, o));
+            if ((threadIdx.x & 31) == 0) emax_w[threadIdx.x >> 5] = em;
+            __syncthreads();
+            em = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) em = max(em, emax_w[w]);
+            // scale 2^-e brings the largest finite entry to [2^63, 2^64) (no
+            // scaling of a zero row or of one with an inf or NaN, which then
+            // spreads through the row as in an FP64 transform)
+            e = (em == 0 || em == 0x7ff) ? 0 : em - 1023 - 63;
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const double2 v = raw[k];
+                sh_put(A, Lp, k, fc{ff_split_scaled(v.x, e), ff_split_scaled(v.y, e)});
+            }
         }
         __syncthreads();
         int Ns = 1;
@@ -320,10 +381,32 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
             B = t;
             __syncthreads();
         }
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const fc v = sh_get(A, Lp, k);
-            d[k] = make_double2(ff_to_double_scaled(v.r.x, v.r.y, e),
-                                ff_to_double_scaled(v.i.x, v.i.y, e));
+        if (p.unpack_out) {
+            // fused unpack: real and imaginary parts to their planes, with the
+            // largest |value| for the fixed-point gather
+            const bool has_im = 2 * q + 1 < p.npl_out;
+            unsigned long long m = 0;
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const fc v = sh_get(A, Lp, k);
+                const double re = ff_to_double_scaled(v.r.x, v.r.y, e);
+                p.unpack_out[off_re + k] = re;
+                m = max(m, (unsigned long long)__double_as_longlong(fabs(re)));
+                if (has_im) {
+                    const double im = ff_to_double_scaled(v.i.x, v.i.y, e);
+                    p.unpack_out[off_im + k] = im;
+                    m = max(m, (unsigned long long)__double_as_longlong(fabs(im)));
+                }
+            }
+            if (p.gmax) {
+                for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(~0u, m, o));
+                if ((threadIdx.x & 31) == 0 && m) atomicMax(p.gmax, m);
+            }
+        } else {
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const fc v = sh_get(A, Lp, k);
+                d[k] = make_double2(ff_to_double_scaled(v.r.x, v.r.y, e),
+                                    ff_to_double_scaled(v.i.x, v.i.y, e));
+            }
         }
         // the next row reuses both buffers and emax_w
         A = fsh;

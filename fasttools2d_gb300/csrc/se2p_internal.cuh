@@ -408,6 +408,18 @@ struct FftRowsFF {
     // ceil(2^32 / Ns) of each stage (Ns = product of the earlier radices):
     // j / Ns = umulhi(j, magic) exactly for j Ns < 2^32
     unsigned magic[kFftFFMaxStages] = {};
+    // Optional fused pack (first forward pass) / unpack (last inverse pass):
+    // row r = (pair q = r / Mx, x = r % Mx) is read from / written to two real
+    // planes of G words, re = plane 2q, im = plane 2q+1 (zero / dropped when
+    // 2q+1 >= npl), row x of a plane at x L.
+    int Mx = 0;
+    int64_t G = 0;
+    const void *pack_in = nullptr;    // int64 planes at scale 2^S (bound), or doubles
+    const unsigned long long *bound = nullptr;   // spread bound slot; null or all ones: doubles
+    int npl_in = 0;
+    double *unpack_out = nullptr;     // double planes
+    int npl_out = 0;
+    unsigned long long *gmax = nullptr;   // largest |value| unpacked (bit pattern), optional
 };
 bool fft_rows_ff_plan(int L, FftRowsFF &p);
 void fft_rows_ff_twiddles(int L, float4 *host);   // exp(-2 pi i m/L), m < L, float-float
@@ -450,6 +462,21 @@ cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t 
 // per-bin sums of |coefficients|, then int64 accumulation into a.grid
 // (reinterpreted as long long), and the pack that turns those grids into the
 // complex pairs of the forward FFT.
+// Bound-slot mark of the fixed-point spread: the FP64 spread ran instead and
+// the grids hold doubles.
+constexpr unsigned long long kFixedOff = ~0ull;      // above every finite bound
+
+// Scale S of the fixed-point spread's grids (int64 at 2^S, bound 2^S < 2^59),
+// from the bit pattern of the positive bound.
+__device__ __forceinline__ int fix_shift(unsigned long long bits)
+{
+    if (bits == kFixedOff) return 0;
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex == 0 || ex == 0x7ff) return 0;            // zero (no sources) or not finite
+    const int S = 59 - (ex - 1022);                  // bound < 2^(ex-1022)
+    return S < -960 ? -960 : (S > 960 ? 960 : S);
+}
+
 // ws: 2 nb + 1 doubles, nb = spread_bins(Mx, P) * spread_bins(My, P): the
 // per-bin sums of max_c |c|, the bound slot at ws + nb, then nb int counts.
 // mult is the number of times one stencil can cover a node (> 1 when M <= P)

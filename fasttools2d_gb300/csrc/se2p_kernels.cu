@@ -1288,8 +1288,6 @@ template __global__ void k_real_adj<true, true, kFormFF>(RealArgs);
 // atomics (executed in L2, off the SM's FP64 pipe).
 // ===========================================================================
 constexpr int kSpreadWarps = 8;
-// Bound-slot mark of the fixed-point spread (below): FP64 spread instead.
-constexpr unsigned long long kFixedOff = ~0ull;      // above every finite bound
 // Bit patterns of |g| at or above this are infinities and NaNs.
 constexpr unsigned long long kGridNonFinite = 0x7ff0000000000000ull;
 
@@ -1413,15 +1411,6 @@ template __global__ void k_spread<5>(SpreadArgs);
 // ===========================================================================
 constexpr int kFixedMaxCover = 1 << 14;
 
-// S with bound * 2^S < 2^59, from the bit pattern of the positive bound.
-__device__ __forceinline__ int fix_shift(unsigned long long bits)
-{
-    if (bits == kFixedOff) return 0;
-    const int ex = (int)((bits >> 52) & 0x7ff);
-    if (ex == 0 || ex == 0x7ff) return 0;            // zero (no sources) or not finite
-    const int S = 59 - (ex - 1022);                  // bound < 2^(ex-1022)
-    return S < -960 ? -960 : (S > 960 ? 960 : S);
-}
 
 int spread_bins(int M, int P)
 {
