@@ -552,13 +552,15 @@ struct Io {
 };
 
 // Spread with integer accumulation (k_spread_fix) when the source Gaussian's
-// x and y factors stay below 2^8: sets kY (2^kY bounds each factor) and kfac
+// x and y factors stay below 2^3: sets kY (2^kY bounds each factor) and kfac
 // (the factor of the bin bound).  The factors exceed 1 only when w differs
-// from h P/2; by at most exp(2 |a| h (h P/2 - w)).
+// from h P/2, by at most exp(2 |a| h (h P/2 - w)); the bound grows by 2^(2 kY),
+// so the integer unit coarsens with it (kY = 3, w = 0.7 h P/2: 8e-14 from
+// the FP64 spread), and beyond that the FP64 spread runs.
 static bool spread_fixed_ok(const SpreadArgs &sa, int &kY, double &kfac, int &mult)
 {
     const double wf = std::exp(-2.0 * sa.a * sa.h * std::max(0.0, sa.h * sa.P / 2 - sa.w));
-    if (!(wf <= 256.0)) return false;
+    if (!(wf <= 8.0)) return false;
     kY = 0;
     if (wf > 1.5) {
         int e = 0;

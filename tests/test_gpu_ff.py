@@ -141,8 +141,8 @@ def _kspace_pair(ft, plans, p, q, f, n, xi, eta, M, w, P):
     return out
 
 
-SPREAD_CASES = ["uniform", "clusters", "decades", "w_small", "grid_le_P", "crowded_grid_le_P",
-                "crowded_cluster"]
+SPREAD_CASES = ["uniform", "clusters", "decades", "w_small", "w_tiny", "grid_le_P",
+                "crowded_grid_le_P", "crowded_cluster"]
 
 
 def spread_case(case):
@@ -163,7 +163,9 @@ def spread_case(case):
     elif case == "decades":
         f = f * 10.0 ** rng.uniform(-8, 8, N)
     elif case == "w_small":
-        w = 0.7 * h * P / 2                             # x, y factors up to ~2^3
+        w = 0.7 * h * P / 2                             # x, y factors up to 5.8 (integer spread)
+    elif case == "w_tiny":
+        w = 0.4 * h * P / 2                             # factors up to 34: the FP64 spread runs
     elif case in ("grid_le_P", "crowded_grid_le_P"):
         M, P, xi = 16, 24, 4.0
         w = (1.0 / M) * P / 2
