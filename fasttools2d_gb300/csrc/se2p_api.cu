@@ -38,7 +38,6 @@ enum Slot {
     S_GRID, S_SPEC, S_E1, S_ZPART, S_ZM, S_COUNTERS,
     S_OUT0, S_OUT1, S_OUT2, S_OUT3,             // staged outputs
     S_IN_W1, S_IN_W2, S_WCOEF, S_GR, S_GK, S_SBOXS, S_ZEROS,   // adjoint
-    S_FTAB,                                     // cached per-mode filter factors
     S_GTAB, S_COEF_FF,                          // float-float real space
     S_ZGRID,                                    // complex pairs of grids (1D-pass FFT)
     S_GCOUNT, S_GTGT, S_GMETA,                  // geometry build scratch
@@ -81,8 +80,7 @@ struct se2p_plan_st {
     bool overlap = true;             // real space concurrent with the k-space chain
     bool timing = false;
     bool count_pairs = false;
-    double ftab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // (Mx, My, Lx, Ly, xi, eta, layout) of S_FTAB
-    double mtab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // the same for S_MTAB
+    double mtab_key[7] = {0, 0, 0, 0, 0, 0, -1};   // (Mx, My, Lx, Ly, xi, eta, layout) of S_MTAB
     bool gtab_ready = false;                   // S_GTAB holds the E1 fit
     // float-float FFT twiddles: the length and device copy each slot holds,
     // and the host tables the (asynchronous) uploads read from
@@ -337,29 +335,11 @@ int get_fft(se2p_plan pl, cudaStream_t st, int Mx, int My, int batch, int dir, c
     return SE2P_OK;
 }
 
-// Per-mode filter factors depend only on (Mx, My, Lx, Ly, xi, eta); the plan
-// keeps them between calls, like cuFFT keeps its twiddles.
-int filter_table(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
-{
-    const double key[7] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta,
-                           (double)fa.transposed};
-    const size_t H = (size_t)fa.Mx * (fa.My / 2 + 1);
-    const bool have = pl->buf[S_FTAB].p && pl->buf[S_FTAB].bytes >= H * sizeof(double2) &&
-                      memcmp(key, pl->ftab_key, sizeof key) == 0;
-    double2 *tab = nullptr;
-    CKS(ensure_t(pl, S_FTAB, H, &tab));
-    if (!have) {
-        fa.etab = nullptr;
-        CK(launch_filter_table(fa, tab, st, pl->launches));
-        memcpy(pl->ftab_key, key, sizeof key);
-    }
-    fa.etab = tab;
-    return SE2P_OK;
-}
-
-// The forward filter's effective per-mode multipliers (k_filter_matrix_table),
-// kept like the factor table; k_filter then does two small complex mat-vecs
-// per mode (20 FP64 operations instead of about 60).
+// The filters' effective per-mode multipliers (k_filter_matrix_table) depend
+// only on (Mx, My, Lx, Ly, xi, eta) and the layout; the plan keeps them
+// between calls, like cuFFT keeps its twiddles.  k_filter and k_filter_adj
+// then do two small complex mat-vecs per mode (about 20 FP64 operations
+// instead of 60).
 int filter_matrix(se2p_plan pl, FilterArgs &fa, cudaStream_t st)
 {
     const double key[7] = {(double)fa.Mx, (double)fa.My, fa.Lx, fa.Ly, fa.xi, fa.eta,
@@ -1025,7 +1005,6 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.dlp_in = J.dlp ? doff : -1;
         fa.slp_out = 0;
         fa.dlp_out = J.slp ? 2 : 0;
-        fa.etab = nullptr;
         fa.transposed = 1;
         {
             StageTimer tm(pl, T_FILTER, ks);
@@ -1313,11 +1292,10 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     fa.slp_out = 0;
     fa.dlp_in = 2;
     fa.dlp_out = 2;
-    fa.etab = nullptr;
     fa.transposed = 1;
     {
         StageTimer tm(pl, T_FILTER, ks);
-        CKS(filter_table(pl, fa, ks));
+        CKS(filter_matrix(pl, fa, ks));
         CK(launch_filter_adj(fa, ks, pl->launches));
     }
     {

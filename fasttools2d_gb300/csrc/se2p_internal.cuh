@@ -312,7 +312,6 @@ struct FilterArgs {
     double Lx, Ly, xi, eta, scale;   // scale = 1 / (Mx My)
     int slp_in, dlp_in;         // first spectrum of each kind (-1 = absent)
     int slp_out, dlp_out;       // where the 2 filtered spectra of each kind go
-    const double2 *etab;        // per-mode (SLP e, DLP e*t) from k_filter_table, or NULL
     int transposed = 0;         // spectra stored [c][ky][x] (x fastest) instead of [c][x][ky]
     // per-mode effective multipliers from k_filter_matrix_table (forward
     // filter only), or NULL: kFilterMat doubles per mode
@@ -492,8 +491,6 @@ cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
                                     const unsigned long long *bound, double2 *z, cudaStream_t st,
                                     int64_t &launches);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t st, int64_t &launches);
-cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
-                                int64_t &launches);
 cudaError_t launch_filter_matrix_table(const FilterArgs &a, double *mtab, cudaStream_t st,
                                        int64_t &launches);
 cudaError_t launch_gather(const GatherArgs &a, int nc, cudaStream_t st, int64_t &launches);

@@ -694,12 +694,14 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         __syncwarp();
         const int total = W.nbp[9];
         ncand += (unsigned)total;
+        int kc = 0;   // neighbour box of this lane's candidate (v only grows)
         for (int v0 = 0; v0 < total; v0 += 32) {
             const int v = v0 + lane;
-            int fl = 0, s = 0, k = 0;
+            int fl = 0, s = 0, k = kc;
             bool nearp = false;
             if (v < total) {
                 while (v >= W.nbp[k + 1]) k++;
+                kc = k;
                 s = W.nbs[k] + (v - W.nbp[k]);
                 if (k == 0) {
                     // own box, no cutoff.  Distinct FP32 images imply an FP64
@@ -1190,12 +1192,14 @@ __global__ void __launch_bounds__(kAdjWarps * 32, 5) k_real_adj(RealArgs a)
         if (lane == 0) W.nbp[0] = 0;
         __syncwarp();
         const int total = W.nbp[9];
+        int kc = 0;   // neighbour box of this lane's candidate (vi only grows)
         for (int v0 = 0; v0 < total; v0 += 32) {
             const int vi = v0 + lane;
-            int fl = 0, t = 0, k = 0;
+            int fl = 0, t = 0, k = kc;
             bool nearp = false;
             if (vi < total) {
                 while (vi >= W.nbp[k + 1]) k++;
+                kc = k;
                 t = W.nbs[k] + (vi - W.nbp[k]);
                 if (k == 0) {
                     const double2 T = a.tp[t];
@@ -1849,9 +1853,8 @@ __global__ void k_filter(FilterArgs a)
     const double k2p = (jy == a.My / 2) ? k2 : -k2;
     const double sc = a.scale;
     double2 so1, so2, do1, do2;
-    // the factors depend on K^2, which k and its partner share; a zero or
-    // non-finite factor (the zero mode) is recomputed inline and discarded
-    const double2 ft = a.etab ? a.etab[idx] : make_double2(-1.0, -1.0);
+    // (without the cached multipliers: the factors computed here)
+    const double2 ft = make_double2(-1.0, -1.0);
     if (a.slp_in >= 0) {
         const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
         slp_mode(k1, k2, a.xi, a.eta, h1, h2, so1, so2, ft.x);
@@ -1887,31 +1890,6 @@ __global__ void k_filter(FilterArgs a)
         sp[a.dlp_out * G + idx] = do1;
         sp[(a.dlp_out + 1) * G + idx] = do2;
     }
-}
-
-// Per-mode (SLP factor, DLP factor) for the cached filter table; the zero
-// mode, where the factors are not finite, stores -1 (compute inline).
-__global__ void k_filter_table(FilterArgs a, double2 *tab)
-{
-    const int H = a.My / 2 + 1;
-    const int64_t G = (int64_t)a.Mx * H;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= G) return;
-    int jx, jy;
-    if (a.transposed) {
-        jy = (int)(idx / a.Mx);
-        jx = (int)(idx - (int64_t)jy * a.Mx);
-    } else {
-        jx = (int)(idx / H);
-        jy = (int)(idx - (int64_t)jx * H);
-    }
-    const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
-    const double K2 = k1 * k1 + k2 * k2;
-    if (jx == 0 && jy == 0) {
-        tab[idx] = make_double2(-1.0, -1.0);
-        return;
-    }
-    tab[idx] = make_double2(slp_factor(K2, a.xi, a.eta), dlp_factor(K2, a.xi, a.eta));
 }
 
 // Per-mode effective multipliers of k_filter (its arithmetic, once per
@@ -2210,6 +2188,28 @@ __global__ void k_filter_adj(FilterArgs a)
         jy = (int)(idx - (int64_t)jx * H);
     }
     double2 *sp = reinterpret_cast<double2 *>(a.spec);
+    if (a.mtab) {
+        // the forward filter's cached multipliers: the SLP matrix (symmetric)
+        // and the DLP rows applied transposed, with the same -i
+        const double *m = a.mtab + (int64_t)kFilterMat * idx;
+        if (a.slp_in >= 0) {
+            const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
+            sp[a.slp_out * G + idx] =
+                make_double2(fma(m[0], h1.x, -m[1] * h2.x), fma(m[0], h1.y, -m[1] * h2.y));
+            sp[(a.slp_out + 1) * G + idx] =
+                make_double2(fma(m[2], h2.x, -m[1] * h1.x), fma(m[2], h2.y, -m[1] * h1.y));
+        }
+        if (a.dlp_in >= 0) {
+            const double2 p1 = sp[a.dlp_in * G + idx], p2 = sp[(a.dlp_in + 1) * G + idx];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double re = fma(m[3 + c], p1.x, m[6 + c] * p2.x);
+                const double im = fma(m[3 + c], p1.y, m[6 + c] * p2.y);
+                sp[(a.dlp_out + c) * G + idx] = make_double2(im, -re);
+            }
+        }
+        return;
+    }
     const bool zero = (jx == 0 && jy == 0);
     const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
     const double k1 = kfreq(jx, a.Mx, a.Lx), k2 = kfreq(jy, a.My, a.Ly);
@@ -2219,7 +2219,7 @@ __global__ void k_filter_adj(FilterArgs a)
     if (a.slp_in >= 0) {
         double2 o1, o2;
         const double2 h1 = sp[a.slp_in * G + idx], h2 = sp[(a.slp_in + 1) * G + idx];
-        const double fe = a.etab ? a.etab[idx].x : -1.0;
+        const double fe = -1.0;                      // computed in slp_mode
         slp_mode(k1, k2, a.xi, a.eta, h1, h2, o1, o2, fe);
         if (nyq) {
             double2 p1, p2;
@@ -2633,15 +2633,6 @@ cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t 
     case 4: k_spread<4><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     default: k_spread<5><<<g, kSpreadWarps * 32, 0, st>>>(a); break;
     }
-    launches++;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_filter_table(const FilterArgs &a, double2 *tab, cudaStream_t st,
-                                int64_t &launches)
-{
-    const int64_t n = (int64_t)a.Mx * (a.My / 2 + 1);
-    k_filter_table<<<grid_for(n, 256), 256, 0, st>>>(a, tab);
     launches++;
     return cudaGetLastError();
 }
