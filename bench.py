@@ -509,10 +509,7 @@ def gpu_arm(args, rank, world, local_rank):
         step_device()
     torch.cuda.synchronize(dev)
 
-    # ---- device-resident timed region -------------------------------------
-    plan.enable_timing(True)
-    plan.stage_times(reset=True)
-    plan.count_pairs(True, reset=True)
+    # ---- device-resident timed region (no stage events, no pair counters) --
     launches0 = plan.kernel_launches
     gpu_id = local_rank
     try:
@@ -525,9 +522,6 @@ def gpu_arm(args, rank, world, local_rank):
         total_ms = timed(step_device, args.steps)
         barrier()
     launches = plan.kernel_launches - launches0
-    counts = plan.count_pairs(False, reset=True)
-    stages = plan.stage_times(reset=True)
-    plan.enable_timing(False)
     total_ms, value = aggregate_replicas(total_ms, args.steps, world, dev)
     ms_per_step = total_ms / args.steps
 
@@ -544,12 +538,17 @@ def gpu_arm(args, rank, world, local_rank):
     # ---- per-kernel times without overlap (for the roofline) -------------
     # Real space normally runs concurrently with the k-space chain; for the
     # per-kernel roofline the stages are timed once more, in order.
+    # The real-space pair counters run here too (they add ballots to the
+    # candidate loop, so the timed region above runs without them).
     plan.set_overlap(False)
     plan.enable_timing(True)
     plan.stage_times(reset=True)
-    for _ in range(2):
+    plan.count_pairs(True, reset=True)
+    n_serial = 2
+    for _ in range(n_serial):
         step_device()
     torch.cuda.synchronize(dev)
+    counts = plan.count_pairs(False, reset=True)
     stages = plan.stage_times(reset=True)
     plan.enable_timing(False)
     plan.set_overlap(True)
@@ -574,7 +573,7 @@ def gpu_arm(args, rank, world, local_rank):
     own = {k: per[k] for k in ("real", "spread", "gather", "filter") if k in per}
     top = max(own, key=own.get)
     top_ms = own[top]
-    pairs_per_launch = (counts[1] + counts[2]) / args.steps     # counted in the timed region
+    pairs_per_launch = (counts[1] + counts[2]) / n_serial       # counted in the serialised pass
     evals_per_launch = pairs_per_launch / 2                     # SLP and DLP share each evaluation
     clock_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -606,7 +605,7 @@ def gpu_arm(args, rank, world, local_rank):
                  "ms_per_launch": top_ms, "top_stage": top,
                  "real_space": {"ms_per_launch": per.get("real"),
                                 "accepted_pairs_per_launch": pairs_per_launch,
-                                "candidates_per_launch": counts[0] / args.steps,
+                                "candidates_per_launch": counts[0] / n_serial,
                                 "pairs_per_s": pairs_per_launch / (per["real"] * 1e-3)
                                 if "real" in per else None}})
     stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1] > 0}

@@ -254,6 +254,7 @@ struct RealWarp {
     int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
     double2 nbz[9];
     float2 nbzf[9];
+    float2 nbe[9];              // 2^-22 (|t| + |z|) per neighbour box (the pre-test band)
     // FP32-grid form: target position as float-float (hi.x, hi.y, lo.x, lo.y)
     float4 tposff[kRing];
 };
@@ -681,7 +682,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
             const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
             const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
             W.nbz[lane] = make_double2(zx, zy);
-            W.nbzf[lane] = make_float2((float)zx, (float)zy);
+            const float zxf = (float)zx, zyf = (float)zy;
+            W.nbzf[lane] = make_float2(zxf, zyf);
+            W.nbe[lane] = make_float2(0x1p-22f * (fabsf(Tf.x) + fabsf(zxf)),
+                                      0x1p-22f * (fabsf(Tf.y) + fabsf(zyf)));
         }
         int incl = cntk;
 #pragma unroll
@@ -737,8 +741,9 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
                     const float r2f = dxf * dxf + dyf * dyf;
                     // |r2f - r2| bound for both offset forms (3 roundings per
                     // coordinate, then squaring and summing), doubled.
-                    const float ex = 0x1p-22f * (fabsf(Sf.x) + fabsf(Tf.x) + fabsf(zf.x));
-                    const float ey = 0x1p-22f * (fabsf(Sf.y) + fabsf(Tf.y) + fabsf(zf.y));
+                    const float2 nbe = W.nbe[k];
+                    const float ex = fmaf(0x1p-22f, fabsf(Sf.x), nbe.x);
+                    const float ey = fmaf(0x1p-22f, fabsf(Sf.y), nbe.y);
                     const float band = 2.0f * (ex * (2.0f * fabsf(dxf) + ex) +
                                                ey * (2.0f * fabsf(dyf) + ey) + 0x1p-22f * r2f);
                     const float xf = r2f * a.xi2f;
@@ -764,8 +769,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
             }
             if (!SLP) fl &= 2;
             if (!DLP) fl &= 1;
-            nslp += __popc(__ballot_sync(~0u, (fl & 1) != 0));
-            ndlp += __popc(__ballot_sync(~0u, (fl & 2) != 0));
+            if (a.counters) {                        // (warp-uniform)
+                nslp += __popc(__ballot_sync(~0u, (fl & 1) != 0));
+                ndlp += __popc(__ballot_sync(~0u, (fl & 2) != 0));
+            }
             const int2 ent = make_int2(s, slot | (k << 8) | (fl << 12));
 #pragma unroll
             for (int j = 0; j < 2; j++) {
