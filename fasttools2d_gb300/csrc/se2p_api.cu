@@ -517,6 +517,9 @@ struct Job {
     bool real = false, kspace = false; // which parts
     bool wrap = false;                 // wrap points first (driver composites)
     bool zero_mode = false;            // DLP k=0 term
+    // the plan's wrapped and sorted copies already hold these points (the
+    // k-space runs of one geometry apply after its first): skip wrap and sort
+    bool reuse_sort = false;
     double xi = 0, eta = 0, w = 0, Lx = 0, Ly = 0;
     int nx = 1, ny = 1, Mx = 0, My = 0, P = 0;
 };
@@ -731,7 +734,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
 
     // Wrapped positions (driver composites); the raw sources stay for the zero mode.
     const double2 *ws = ps, *wt = pt;
-    if (J.wrap) {
+    if (J.wrap && !J.reuse_sort) {
         StageTimer tm(pl, T_WRAP);
         double2 *a = nullptr, *b = nullptr;
         if (ns > 0) {
@@ -778,7 +781,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             CKS(ensure_t(pl, S_TPL, ntz, &tpl));
         }
     }
-    {
+    if (!J.reuse_sort) {
     StageTimer tm(pl, T_SORT);
     BinArgs bs{ws, ns, J.Lx, J.Ly, nx, ny, sbox, srank, count};
     CK(launch_bin(bs, sstart, nbox, sperm, nullptr, sp, spf, st, pl->launches, spl));
@@ -923,6 +926,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         fa.xi = J.xi;
         fa.eta = J.eta;
         fa.scale = (float)(1.0 / ((double)Mx * (double)My));
+        fa.c1 = (float)(0.25 / (J.xi * J.xi));
+        fa.c2 = (float)(0.25 * (1 - J.eta) / (J.xi * J.xi));
+        fa.dkx = 2.0 * kPi / J.Lx;
+        fa.dky = 2.0 * kPi / J.Ly;
         fa.slp_in = J.slp ? 0 : -1;
         fa.dlp_in = J.dlp ? doff : -1;
         fa.slp_out = 0;
@@ -1902,6 +1909,7 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
             J.slp = g->slp;
             J.dlp = g->dlp;
             J.zero_mode = g->dlp;
+            J.reuse_sort = r0 + r > 0;               // same points as the first RHS's run
             Io io;
             io.psrc = reinterpret_cast<const double *>(g->ps);
             io.ptar = reinterpret_cast<const double *>(g->pt);

@@ -352,6 +352,10 @@ struct FilterArgsF {
     int Mx, My;
     double Lx, Ly, xi, eta;
     float scale;
+    // from the host, as FP64 division is slow on the device: 1/(4 xi^2),
+    // (1 - eta)/(4 xi^2) and the wavenumber steps 2 pi / L
+    float c1, c2;
+    double dkx, dky;
     int slp_in, dlp_in, slp_out, dlp_out;
 };
 

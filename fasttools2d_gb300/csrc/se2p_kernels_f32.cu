@@ -113,9 +113,10 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
 // FP32 filter on the half spectrum; same modes, Nyquist projection, -i and
 // 1/(Mx My) as k_filter (se2p_kernels.cu).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float kfreq_f(int j, int M, double L)
+// dk = 2 pi / L, formed on the host
+__device__ __forceinline__ float kfreq_f(int j, int M, double dk)
 {
-    return (float)(2.0 * kPi / L * (double)(j <= M / 2 ? j : j - M));
+    return (float)(dk * (double)(j <= M / 2 ? j : j - M));
 }
 
 __device__ __forceinline__ void slp_mode_f(float k1, float k2, float c1, float c2, float2 h1,
@@ -151,14 +152,15 @@ __global__ void k_filter_f32(FilterArgsF a)
     const int64_t G = (int64_t)a.Mx * H;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G) return;
-    const int jx = (int)(idx / H), jy = (int)(idx - (int64_t)jx * H);
+    const int jx = (int)((unsigned long long)idx / (unsigned)H);
+    const int jy = (int)(idx - (int64_t)jx * H);
     float2 *sp = a.spec;
     const bool zero = (jx == 0 && jy == 0);
     const bool nyq = (jx == a.Mx / 2) || (jy == a.My / 2);
-    const float k1 = kfreq_f(jx, a.Mx, a.Lx), k2 = kfreq_f(jy, a.My, a.Ly);
+    const float k1 = kfreq_f(jx, a.Mx, a.dkx), k2 = kfreq_f(jy, a.My, a.dky);
     const float k1p = (jx == a.Mx / 2) ? k1 : -k1;
     const float k2p = (jy == a.My / 2) ? k2 : -k2;
-    const float c1 = (float)(0.25 / (a.xi * a.xi)), c2 = (float)(0.25 * (1 - a.eta) / (a.xi * a.xi));
+    const float c1 = a.c1, c2 = a.c2;
     const float sc = a.scale;
     float2 so1, so2, do1, do2;
     if (a.slp_in >= 0) {
