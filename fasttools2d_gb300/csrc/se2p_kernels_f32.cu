@@ -53,6 +53,9 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int P1 = a.P + 1, NN = P1 * P1;
     const size_t G = (size_t)a.Mx * a.My;
+    // (i, jj) of flattened stencil entry q = lane + 32 k, stepped without division
+    const int di = 32 / P1, dj = 32 - di * P1, i0 = lane / P1, j0 = lane - i0 * P1;
+    const bool once = a.Mx > a.P && a.My > a.P;      // a stencil wraps at most once
     const int64_t nw = (int64_t)gridDim.x * kSpreadWarpsF;
     for (int64_t base = ((int64_t)blockIdx.x * kSpreadWarpsF + wid) * 32; base < a.ns;
          base += nw * 32) {
@@ -89,9 +92,21 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
                 wsh[wid][NC][lane] = axis_weight(y0, y1, y2, lane);
             }
             __syncwarp();
-            for (int qd = lane; qd < NN; qd += 32) {
-                const int i = qd / P1, jj = qd - i * P1;
-                const int col = wrapi(smx + i, a.Mx), row = wrapi(smy + jj, a.My);
+            const int c0 = wrapi(smx, a.Mx), r0 = wrapi(smy, a.My);
+            int i = i0, jj = j0;
+            for (int qd = lane; qd < NN; qd += 32, i += di, jj += dj) {
+                if (jj >= P1) {
+                    jj -= P1;
+                    i++;
+                }
+                int col = c0 + i, row = r0 + jj;
+                if (once) {
+                    col = col >= a.Mx ? col - a.Mx : col;
+                    row = row >= a.My ? row - a.My : row;
+                } else {
+                    col %= a.Mx;
+                    row %= a.My;
+                }
                 const float wy = wsh[wid][NC][jj];
                 const size_t node = (size_t)col * a.My + row;
                 if (NC == 2) {
