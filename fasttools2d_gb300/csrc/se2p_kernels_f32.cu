@@ -4,31 +4,30 @@
 // For tolerances >= 1e-6 the grid work runs in FP32: GB300 issues FP32 at
 // ~58x its FP64 rate, so these kernels become bound by atomics and memory
 // instead of the FP64 pipe.  Discrete decisions stay exactly the reference's:
-// the stencil origin (FindClosestNode) and the in-cell offsets are computed
-// in FP64; so is the exponent of every Gaussian weight, as a quadratic in the
-// node index i,
-//   a (p^2 + 2 w p) + a h^2 (i - P/2)^2 - 2 a h p i      (a = -2 xi^2 / eta)
-// -- the fast-Gaussian-gridding factorisation of
-// PE/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:64-67, :95-99 summed in the
-// exponent -- and only the exponential and the grid arithmetic run in FP32.
+// the stencil origin (FindClosestNode) and the in-cell offset p are computed
+// in FP64.  The exponent of the fast-Gaussian-gridding weights
+// (PE/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:64-67, :95-99),
+//   a (p^2 + 2 w p) + a h^2 (i - P/2)^2 - 2 a h p i      (a = -2 xi^2 / eta),
+// is regrouped as a (p - h (i - P/2))^2 + 2 a p (w - h P/2): the second term
+// is a per-point factor (1 when w = h P/2), taken once in FP64, and the
+// first is formed in FP32.  Its rounding moves a weight e^-x by about
+// x e^-x 2^-22 <= 1e-7 of the largest weight, well inside the form's 1e-6.
 #include "se2p_internal.cuh"
 
 namespace se2p {
 
-// Per-axis exponent coefficients: e(i) = A0 + i (A1 + i A2).
-__device__ __forceinline__ void axis_coef(double p, double a, double w, double h, int P,
-                                          double &A0, double &A1, double &A2)
+// The per-point factor exp(2 a p (w - h P/2)) of one axis (FP64; 1 when w = h P/2).
+__device__ __forceinline__ double axis_factor(double p, double a, double w, double h, int P)
 {
-    const double c = (double)(P / 2);
-    A2 = a * h * h;
-    A1 = -2.0 * a * h * (h * c + p);
-    A0 = a * (p * p + 2.0 * w * p) + A2 * c * c;
+    const double dw = w - h * (double)(P / 2);
+    return dw == 0.0 ? 1.0 : exp(2.0 * a * p * dw);
 }
 
-__device__ __forceinline__ float axis_weight(double A0, double A1, double A2, int i)
+// exp(a (p - h (i - P/2))^2) in FP32 (af = a, hf = h, pf = p as floats).
+__device__ __forceinline__ float axis_weight(float af, float hf, float pf, int P, int i)
 {
-    const double di = (double)i;
-    return __expf((float)fma(di, fma(di, A2, A1), A0));
+    const float d = fmaf(-hf, (float)(i - P / 2), pf);
+    return __expf(af * d * d);
 }
 
 __device__ __forceinline__ int wrapi(int i, int M)
@@ -47,7 +46,7 @@ __device__ __forceinline__ int wrapi(int i, int M)
 constexpr int kSpreadWarpsF = 8;
 
 template <int NC>
-__global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a)
+__global__ void __launch_bounds__(kSpreadWarpsF * 32, 4) k_spread_f32(SpreadArgsF a)
 {
     __shared__ float wsh[kSpreadWarpsF][NC + 1][32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -61,7 +60,7 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
          base += nw * 32) {
         const int64_t sl = base + lane;
         int mx = 0, my = 0;
-        double X0 = 0, X1 = 0, X2 = 0, Y0 = 0, Y1 = 0, Y2 = 0;
+        float pxf = 0.f, pyf = 0.f;
         float cf[NC];
 #pragma unroll
         for (int c = 0; c < NC; c++) cf[c] = 0.f;
@@ -69,27 +68,25 @@ __global__ void __launch_bounds__(kSpreadWarpsF * 32) k_spread_f32(SpreadArgsF a
             const double2 S = a.sp[sl];
             double px, py;
             closest_node(S.x, S.y, a.Lhx, a.Lhy, a.h, a.P, mx, my, px, py);
-            axis_coef(px, a.a, a.w, a.h, a.P, X0, X1, X2);
-            // the y factor exp(a (py^2 + 2 w py)) belongs to the same product
-            axis_coef(py, a.a, a.w, a.h, a.P, Y0, Y1, Y2);
+            pxf = (float)px;
+            pyf = (float)py;
+            const double E = axis_factor(px, a.a, a.w, a.h, a.P) * axis_factor(py, a.a, a.w, a.h, a.P);
 #pragma unroll
-            for (int c = 0; c < NC; c++) cf[c] = (float)a.coef[NC * sl + c];
+            for (int c = 0; c < NC; c++) cf[c] = (float)(a.coef[NC * sl + c] * E);
         }
+        const float af = (float)a.a, hf = (float)a.h;
         const int cnt = (int)min((int64_t)32, a.ns - base);
         for (int j = 0; j < cnt; j++) {
             const int smx = __shfl_sync(~0u, mx, j), smy = __shfl_sync(~0u, my, j);
-            const double x0 = __shfl_sync(~0u, X0, j), x1 = __shfl_sync(~0u, X1, j),
-                         x2 = __shfl_sync(~0u, X2, j);
-            const double y0 = __shfl_sync(~0u, Y0, j), y1 = __shfl_sync(~0u, Y1, j),
-                         y2 = __shfl_sync(~0u, Y2, j);
+            const float spx = __shfl_sync(~0u, pxf, j), spy = __shfl_sync(~0u, pyf, j);
             float sc[NC];
 #pragma unroll
             for (int c = 0; c < NC; c++) sc[c] = __shfl_sync(~0u, cf[c], j);
             if (lane < P1) {
-                const float wx = axis_weight(x0, x1, x2, lane);
+                const float wx = axis_weight(af, hf, spx, a.P, lane);
 #pragma unroll
                 for (int c = 0; c < NC; c++) wsh[wid][c][lane] = sc[c] * wx;
-                wsh[wid][NC][lane] = axis_weight(y0, y1, y2, lane);
+                wsh[wid][NC][lane] = axis_weight(af, hf, spy, a.P, lane);
             }
             __syncwarp();
             const int c0 = wrapi(smx, a.Mx), r0 = wrapi(smy, a.My);
@@ -229,13 +226,12 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
     int mx, my;
     double px, py;
     closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
-    double X0, X1, X2, Y0, Y1, Y2;
-    axis_coef(px, a.a, a.w, a.h, P, X0, X1, X2);
-    axis_coef(py, a.a, a.w, a.h, P, Y0, Y1, Y2);
+    const double E = axis_factor(px, a.a, a.w, a.h, P) * axis_factor(py, a.a, a.w, a.h, P);
+    const float af = (float)a.a, hf = (float)a.h, pxf = (float)px, pyf = (float)py;
     float wy[kMaxP + 1];
 #pragma unroll
     for (int j = 0; j <= kMaxP; j++)
-        if (j <= P) wy[j] = axis_weight(Y0, Y1, Y2, j);
+        if (j <= P) wy[j] = axis_weight(af, hf, pyf, P, j);
     float acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) acc[c] = 0.f;
@@ -265,14 +261,14 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
                 for (int c = 0; c < NC; c++) tc[c] = fmaf(wy[j], v[c], tc[c]);
             }
         }
-        const float wx = axis_weight(X0, X1, X2, i);
+        const float wx = axis_weight(af, hf, pxf, P, i);
 #pragma unroll
         for (int c = 0; c < NC; c++) acc[c] = fmaf(wx, tc[c], acc[c]);
     }
+    const double sE = a.scale * E;
 #pragma unroll
     for (int k = 0; k < NC / 2; k++)
-        a.out[k * a.nt + t] = make_double2((double)acc[2 * k] * a.scale,
-                                           (double)acc[2 * k + 1] * a.scale);
+        a.out[k * a.nt + t] = make_double2((double)acc[2 * k] * sE, (double)acc[2 * k + 1] * sE);
 }
 
 // ---------------------------------------------------------------------------
