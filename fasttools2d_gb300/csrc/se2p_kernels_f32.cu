@@ -212,7 +212,7 @@ __global__ void k_filter_f32(FilterArgsF a)
 }
 
 // ---------------------------------------------------------------------------
-// FP32 gather: one lane per target; weights from FP64 exponents, FP32 sums.
+// FP32 gather: one lane per target; FP32 weights and sums (the per-point factor in FP64).
 // The NC grids are interleaved per node ([node][NC], the C2R's strided
 // output), one vector load per node.
 // ---------------------------------------------------------------------------
