@@ -216,21 +216,24 @@ __global__ void k_filter_f32(FilterArgsF a)
 // The NC grids are interleaved per node ([node][NC], the C2R's strided
 // output), one vector load per node.
 // ---------------------------------------------------------------------------
-template <int NC>
-__global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
+// PT > 0: the stencil width as a template constant (PT = P), so the row
+// weights take PT + 1 registers and four blocks fit per SM.
+template <int NC, int PT>
+__global__ void __launch_bounds__(256, 4) k_gather_f32(GatherArgsF a)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nt) return;
-    const int P = a.P;
+    constexpr int PM = PT > 0 ? PT : kMaxP;
+    const int P = PT > 0 ? PT : a.P;
     const double2 T = a.tp[t];
     int mx, my;
     double px, py;
     closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
     const double E = axis_factor(px, a.a, a.w, a.h, P) * axis_factor(py, a.a, a.w, a.h, P);
     const float af = (float)a.a, hf = (float)a.h, pxf = (float)px, pyf = (float)py;
-    float wy[kMaxP + 1];
+    float wy[PM + 1];
 #pragma unroll
-    for (int j = 0; j <= kMaxP; j++)
+    for (int j = 0; j <= PM; j++)
         if (j <= P) wy[j] = axis_weight(af, hf, pyf, P, j);
     float acc[NC];
 #pragma unroll
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(256) k_gather_f32(GatherArgsF a)
 #pragma unroll
         for (int c = 0; c < NC; c++) tc[c] = 0.f;
 #pragma unroll
-        for (int j = 0; j <= kMaxP; j++) {
+        for (int j = 0; j <= PM; j++) {
             if (j <= P) {
                 const int row = rows_inside ? my + j : wrapi(my + j, a.My);
                 float v[NC];
@@ -309,8 +312,13 @@ cudaError_t launch_gather_f32(const GatherArgsF &a, int nc, cudaStream_t st, int
 {
     if (a.nt <= 0) return cudaSuccess;
     const unsigned g = grid_for_f(a.nt, 256);
-    if (nc == 2) k_gather_f32<2><<<g, 256, 0, st>>>(a);
-    else k_gather_f32<4><<<g, 256, 0, st>>>(a);
+    if (a.P == 12) {
+        if (nc == 2) k_gather_f32<2, 12><<<g, 256, 0, st>>>(a);
+        else k_gather_f32<4, 12><<<g, 256, 0, st>>>(a);
+    } else {
+        if (nc == 2) k_gather_f32<2, 0><<<g, 256, 0, st>>>(a);
+        else k_gather_f32<4, 0><<<g, 256, 0, st>>>(a);
+    }
     launches++;
     return cudaGetLastError();
 }
