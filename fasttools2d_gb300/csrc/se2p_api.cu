@@ -1305,9 +1305,18 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
         CKS(filter_matrix(pl, fa, ks));
         CK(launch_filter_adj(fa, ks, pl->launches));
     }
+    // float-float gather (FP64 form) when float's range holds the weights;
+    // it needs the grid maximum from the unpack and reuses zg for its planes
+    unsigned long long *gmax = nullptr;
+    const double a_gauss = -2 * J.xi * J.xi / J.eta;
+    const bool ffg = form == kFormFF && adj_gather_ff_ok(a_gauss, h, J.w, P);
+    if (ffg) {
+        CKS(ensure_t(pl, S_GMAX, 1, &gmax));
+        CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long), ks));
+    }
     {
         StageTimer tm(pl, T_FFT_INV, ks);
-        CKS(fft_inv_1d(pl, ks, Mx, My, spec, 5, zg, grid, ffft));
+        CKS(fft_inv_1d(pl, ks, Mx, My, spec, 5, zg, grid, ffft, gmax));
     }
     GatherAdjArgs ga;
     ga.sp = sp;
@@ -1327,6 +1336,10 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     ga.scale = sg / (4 * kPi);
     ga.e1 = e1;
     ga.out = gk;
+    if (ffg) {
+        ga.gmax = gmax;
+        ga.gff = reinterpret_cast<float2 *>(zg);     // 5 G float2 within its 3 G double2
+    }
     {
         StageTimer tm(pl, T_GATHER, ks);
         CK(launch_gather_adj(ga, ks, pl->launches));

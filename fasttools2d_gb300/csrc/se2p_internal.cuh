@@ -290,6 +290,11 @@ struct GatherAdjArgs {
     double Lhx, Lhy, h, w, a, scale;
     const double *e1;
     double *out;          // 7 per source: 5 values, gradient x, y
+    // float-float form (k_gather_adj_ff): the bit pattern of max |grid|
+    // (from the inverse FFT's unpack) and room for the grids as float-float
+    // planes; null for the FP64 gather alone
+    unsigned long long *gmax = nullptr;
+    float2 *gff = nullptr;
 };
 
 struct SpreadArgs {
@@ -449,6 +454,9 @@ cudaError_t launch_real_adj(const RealArgs &a, bool slp, bool dlp, cudaStream_t 
 cudaError_t launch_sorted_pair(int64_t n, const int *perm, const double2 *a, const double2 *b,
                                double *out, cudaStream_t st, int64_t &launches);
 cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &launches);
+// With a.gff set (adj_gather_ff_ok), the float-float gather runs, and the
+// FP64 one only when the grid holds a non-finite value.
+bool adj_gather_ff_ok(double a, double h, double w, int P);
 cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, const double *gk,
                                 const double *w, int64_t nt, double2 *part,

@@ -2269,6 +2269,8 @@ __global__ void k_filter_adj(FilterArgs a)
 template <int PT>
 __global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
 {
+    // behind k_gather_adj_ff: runs only when the grid held a non-finite value
+    if (a.gff && *a.gmax < kGridNonFinite) return;
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.ns) return;
     const int P = PT > 0 ? PT : a.P;
@@ -2341,6 +2343,214 @@ __global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
 
 template __global__ void k_gather_adj<24>(GatherAdjArgs);
 template __global__ void k_gather_adj<0>(GatherAdjArgs);
+
+// ---------------------------------------------------------------------------
+// The adjoint gather in float-float arithmetic (FP64 form).
+//
+// k_gather_adj spends 10 DFMA per stencil node, at GB300's FP64 rate, and
+// its 255 registers leave one block per SM.  Here a warp takes one source
+// at a time with lane = stencil row j: per column i the lanes load the five
+// grid values of their rows (consecutive, so the loads coalesce) and keep
+//   A_k(j) = sum_i wx_i g_k(i, j),   B_k(j) = sum_i wx'_i g_k(i, j)
+// in float-float (wx' the x derivative of the weight).  Then
+//   value_k = sum_j wy_j A_k(j),  grad_x = sum_j wy_j sum_k c_k B_k(j),
+//   grad_y = sum_j wy'_j sum_k c_k A_k(j),
+// the same sums as k_gather_adj in another order, with warp reductions over
+// the rows.  The weights come from float-float product scans across lanes
+// (lane i holds e3^i) of the per-source factors, which the lanes form in
+// FP64 for 32 sources at a time; the grids are read as float-float planes
+// scaled by a power of two from the grid maximum (k_grid_to_ff), and the
+// coefficients by their own power of two, so that float's exponent range
+// holds every factor (adj_gather_ff_ok bounds the weights' exponents).
+// The result carries about 2^-44 relative error, against the adjoint's
+// finite-difference checks at 1e-6.
+// ---------------------------------------------------------------------------
+constexpr int kAdjFFWarps = 8;
+
+// 2^sg brings max |grid| below 1.
+__device__ __forceinline__ int ff_grid_shift(unsigned long long gb)
+{
+    if (gb == 0) return 0;
+    return -((int)((gb >> 52) & 0x7ff) - 1022);
+}
+
+__global__ void k_grid_to_ff(const double *__restrict__ grid, int64_t n,
+                             const unsigned long long *__restrict__ gmax, float2 *__restrict__ out)
+{
+    const unsigned long long gb = *gmax;
+    if (gb >= kGridNonFinite) return;
+    const double sc = ldexp(1.0, ff_grid_shift(gb));
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = ff_split(grid[i] * sc);
+}
+
+// acc + w * v, all float-float.
+__device__ __forceinline__ float2 ff_fma(float2 w, float2 v, float2 acc)
+{
+    const float p = w.x * v.x;
+    float e = fmaf(w.x, v.x, -p);
+    e = fmaf(w.x, v.y, e);
+    e = fmaf(w.y, v.x, e);
+    float s, t;
+    two_sum(acc.x, p, s, t);
+    t += e + acc.y;
+    float h, l;
+    fast_two_sum(s, t, h, l);
+    return make_float2(h, l);
+}
+
+__device__ __forceinline__ float2 shfl_ff(float2 v, int src)
+{
+    return make_float2(__shfl_sync(~0u, v.x, src), __shfl_sync(~0u, v.y, src));
+}
+
+__device__ __forceinline__ float2 shfl_up_ff(float2 v, int o)
+{
+    return make_float2(__shfl_up_sync(~0u, v.x, o), __shfl_up_sync(~0u, v.y, o));
+}
+
+__device__ __forceinline__ float2 shfl_xor_ff(float2 v, int o)
+{
+    return make_float2(__shfl_xor_sync(~0u, v.x, o), __shfl_xor_sync(~0u, v.y, o));
+}
+
+template <int PT>
+__global__ void __launch_bounds__(kAdjFFWarps * 32, 2) k_gather_adj_ff(GatherAdjArgs a)
+{
+    const unsigned long long gb = *a.gmax;
+    if (gb >= kGridNonFinite) return;                // the FP64 gather runs instead
+    const int sg = ff_grid_shift(gb);
+    const int P = PT > 0 ? PT : a.P, P1 = P + 1;     // P1 <= 31
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const size_t G = (size_t)a.Mx * a.My;
+    const float2 e1l = lane < P1 ? ff_split(a.e1[lane]) : make_float2(0.f, 0.f);
+    const float2 hl = ff_mul_f(ff_split(a.h), (float)lane);    // h * lane
+    const float2 da = ff_split(2.0 * a.a);
+    const int64_t nw = (int64_t)gridDim.x * kAdjFFWarps;
+    for (int64_t base = ((int64_t)blockIdx.x * kAdjFFWarps + wid) * 32; base < a.ns;
+         base += nw * 32) {
+        // per-source factors of this lane's source, in FP64, then float-float
+        const int64_t sl = base + lane;
+        int mx = 0, my = 0, ec = 0;
+        float2 x0 = make_float2(0.f, 0.f), e3x = x0, e3y = x0, qx = x0, qy = x0;
+        float2 c[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) c[k] = x0;
+        if (sl < a.ns) {
+            const double2 S = a.sp[sl];
+            double px, py;
+            closest_node(S.x, S.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
+            x0 = ff_split(exp(a.a * (px * px + py * py + 2.0 * a.w * px)) *
+                          exp(2.0 * a.a * a.w * py));
+            e3x = ff_split(exp(-2.0 * a.a * a.h * px));
+            e3y = ff_split(exp(-2.0 * a.a * a.h * py));
+            qx = ff_split(px + a.w);
+            qy = ff_split(py + a.w);
+            double cm = 0.0, cv[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                cv[k] = a.coef[5 * sl + k];
+                cm = fmax(cm, fabs(cv[k]));
+            }
+            if (cm > 0.0 && cm <= 1.7976931348623157e308) frexp(cm, &ec);   // cm < 2^ec
+#pragma unroll
+            for (int k = 0; k < 5; k++) c[k] = ff_split(ldexp(cv[k], -ec));
+        }
+        const int cnt = (int)min((int64_t)32, a.ns - base);
+        for (int j = 0; j < cnt; j++) {
+            const int smx = __shfl_sync(~0u, mx, j), smy = __shfl_sync(~0u, my, j);
+            const int sec = __shfl_sync(~0u, ec, j);
+            const float2 sx0 = shfl_ff(x0, j);
+            const float2 b3x = shfl_ff(e3x, j), b3y = shfl_ff(e3y, j);
+            const float2 sqx = shfl_ff(qx, j), sqy = shfl_ff(qy, j);
+            float2 sc[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) sc[k] = shfl_ff(c[k], j);
+            // e3^lane by a product scan across lanes
+            float2 px_ = lane >= 1 ? b3x : make_float2(1.f, 0.f);
+            float2 py_ = lane >= 1 ? b3y : make_float2(1.f, 0.f);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float2 tx = shfl_up_ff(px_, o), ty = shfl_up_ff(py_, o);
+                if (lane >= o) {
+                    px_ = ff_mul(px_, tx);
+                    py_ = ff_mul(py_, ty);
+                }
+            }
+            // lane as column i: wx_i, wx'_i; lane as row j: wy_j, wy'_j
+            // (the derivative factor 2a (p + w - h i) of the weight exponent)
+            const float2 wx = ff_mul(ff_mul(sx0, e1l), px_);
+            const float2 wxd = ff_mul(wx, ff_mul(da, ff_sub(sqx, hl)));
+            const float2 wy = ff_mul(e1l, py_);
+            const float2 wyd = ff_mul(wy, ff_mul(da, ff_sub(sqy, hl)));
+            // column sums as Dot2 accumulators (float sum + float error term),
+            // normalised once after the last column
+            float As[5], Ac[5], Bs[5], Bc[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) As[k] = Ac[k] = Bs[k] = Bc[k] = 0.f;
+            const int row = lane < P1 ? wrap_index(smy + lane, a.My) : 0;
+            int col = wrap_index(smx, a.Mx);
+            for (int i = 0; i <= P; i++) {
+                const float2 wxi = shfl_ff(wx, i), wxdi = shfl_ff(wxd, i);
+                if (lane < P1) {
+                    const float2 *g = a.gff + (size_t)col * a.My + row;
+                    float2 v[5];
+#pragma unroll
+                    for (int k = 0; k < 5; k++) v[k] = __ldg(g + k * G);
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        ff_dot_acc(wxi, v[k], As[k], Ac[k]);
+                        ff_dot_acc(wxdi, v[k], Bs[k], Bc[k]);
+                    }
+                }
+                if (++col == a.Mx) col = 0;
+            }
+            float2 A[5], B[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                A[k] = ff_norm(As[k], Ac[k]);
+                B[k] = ff_norm(Bs[k], Bc[k]);
+            }
+            // rows: values, and the gradients through the coefficients
+            float2 r[7], ca = make_float2(0.f, 0.f), cb = ca;
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                r[k] = ff_mul(wy, A[k]);
+                ca = ff_fma(sc[k], A[k], ca);
+                cb = ff_fma(sc[k], B[k], cb);
+            }
+            r[5] = ff_mul(wy, cb);
+            r[6] = ff_mul(wyd, ca);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 7; k++) r[k] = ff_add(r[k], shfl_xor_ff(r[k], o));
+            }
+            if (lane == 0) {
+                double *out = a.out + 7 * (base + j);
+                const double sv = ldexp(a.scale, -sg), sgr = ldexp(a.scale, sec - sg);
+#pragma unroll
+                for (int k = 0; k < 5; k++) out[k] = ff_to_double(r[k]) * sv;
+                out[5] = ff_to_double(r[5]) * sgr;
+                out[6] = ff_to_double(r[6]) * sgr;
+            }
+        }
+    }
+}
+
+template __global__ void k_gather_adj_ff<24>(GatherAdjArgs);
+template __global__ void k_gather_adj_ff<0>(GatherAdjArgs);
+
+// Float range for the float-float adjoint gather: every weight factor's
+// exponent (x0, e3^i up to i = 31, e1) within 80 of 0.
+bool adj_gather_ff_ok(double a, double h, double w, int P)
+{
+    const double ah2 = std::fabs(a) * h * h;
+    const double c = P / 2 + 1;
+    const double m = std::max(std::max(2.0 + 2.0 * std::fabs(w) / h, 62.0), c * c);
+    return ah2 * m <= 80.0;
+}
 
 
 // sum_t w_dlp(t) (the zero-mode term's weight), partial sums per block.
@@ -2770,6 +2980,17 @@ cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &lau
 cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches)
 {
     if (a.ns <= 0) return cudaSuccess;
+    if (a.gff) {
+        const int64_t n = 5 * (int64_t)a.Mx * a.My;
+        k_grid_to_ff<<<grid_for(n, 256), 256, 0, st>>>(a.grid, n, a.gmax, a.gff);
+        const int64_t warps = (a.ns + 31) / 32;
+        const int64_t want = (warps + kAdjFFWarps - 1) / kAdjFFWarps;
+        const int64_t cap = (int64_t)sm_count() * 2;
+        const unsigned gf = (unsigned)(want < cap ? want : cap);
+        if (a.P == 24) k_gather_adj_ff<24><<<gf, kAdjFFWarps * 32, 0, st>>>(a);
+        else k_gather_adj_ff<0><<<gf, kAdjFFWarps * 32, 0, st>>>(a);
+        launches += 2;
+    }
     const unsigned g = grid_for(a.ns, 256);
     if (a.P == 24) k_gather_adj<24><<<g, 256, 0, st>>>(a);
     else k_gather_adj<0><<<g, 256, 0, st>>>(a);
