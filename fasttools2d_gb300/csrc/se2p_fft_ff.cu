@@ -17,7 +17,7 @@
 // for the exponent scan), scaled by a power of two that
 // puts its largest entry near 2^64 (exact; the FFT of a row of L <= 2^13
 // values grows it by at most L), split into float-float pairs with integer
-// operations, transformed by mixed-radix Stockham stages (radices 8, 4, 2,
+// operations, transformed by mixed-radix Stockham stages (radices 8, 4, 6, 2,
 // 7, 5, 3, ping-pong between two shared buffers), and written back as doubles
 // rebuilt with integer operations (float <-> double conversions run at the
 // FP64 rate on GB300).  Twiddles exp(-2 pi i m / L) come from a per-length
@@ -189,6 +189,23 @@ __device__ __forceinline__ void dft<5>(fc *v, float s, const fc *cst) { dft_odd<
 template <>
 __device__ __forceinline__ void dft<7>(fc *v, float s, const fc *cst) { dft_odd<7>(v, s, cst); }
 
+// R = 6 = 2 x 3 by the prime-factor (Good-Thomas) split, with no inner
+// twiddles: 3-point DFTs of inputs (0, 2, 4) and (3, 5, 1), then 2-point
+// DFTs of their outputs, which land at (3 k1 + 4 k2) mod 6.  cst as for R = 3.
+template <>
+__device__ __forceinline__ void dft<6>(fc *v, float s, const fc *cst)
+{
+    fc a[3] = {v[0], v[2], v[4]}, b[3] = {v[3], v[5], v[1]};
+    dft_odd<3>(a, s, cst);
+    dft_odd<3>(b, s, cst);
+    v[0] = fc_add(a[0], b[0]);
+    v[3] = fc_sub(a[0], b[0]);
+    v[4] = fc_add(a[1], b[1]);
+    v[1] = fc_sub(a[1], b[1]);
+    v[2] = fc_add(a[2], b[2]);
+    v[5] = fc_sub(a[2], b[2]);
+}
+
 template <int R>
 __device__ void stage(const float *A, float *B, int L, int Ns, unsigned magic, float s,
                       const float4 *tw)
@@ -204,6 +221,9 @@ __device__ void stage(const float *A, float *B, int L, int Ns, unsigned magic, f
             const fc w = tw_load(tw, m * (L / R), -1.f);   // cos - i sin
             cst[m - 1] = {w.r, ff_neg(w.i)};
         }
+    } else if (R == 6) {
+        const fc w = tw_load(tw, L / 3, -1.f);       // the 3-point constants
+        cst[0] = {w.r, ff_neg(w.i)};
     }
     const int nb = L / R, stride = L / (Ns * R), Lp = sh_len(L);
     for (int j = threadIdx.x; j < nb; j += blockDim.x) {
@@ -370,6 +390,7 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
             switch (R) {
             case 8: stage<8>(A, B, L, Ns, mg, s, tw); break;
             case 4: stage<4>(A, B, L, Ns, mg, s, tw); break;
+            case 6: stage<6>(A, B, L, Ns, mg, s, tw); break;
             case 2: stage<2>(A, B, L, Ns, mg, s, tw); break;
             case 7: stage<7>(A, B, L, Ns, mg, s, tw); break;
             case 5: stage<5>(A, B, L, Ns, mg, s, tw); break;
@@ -425,6 +446,7 @@ bool fft_rows_ff_plan(int L, FftRowsFF &p)
     int n = L;
     while (n % 8 == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = 8; n /= 8; }
     while (n % 4 == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = 4; n /= 4; }
+    while (n % 6 == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = 6; n /= 6; }
     while (n % 2 == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = 2; n /= 2; }
     for (int r : {7, 5, 3})
         while (n % r == 0 && p.nst < kFftFFMaxStages) { p.radix[p.nst++] = r; n /= r; }
