@@ -65,7 +65,7 @@ UNIT = "evals/s"
 # * spread (k_spread_fix, exact int64 sums): bound by L2 atomics; work = one
 #   64-bit reduction per stencil node and grid, (P+1)^2 C_in per source with
 #   C_in = 5 grids (SLP f1, f2; DLP S11, S12+S21, S22); peak = coalesced int64
-#   atomics measured in this run (torch index_add_).
+#   atomics measured in this run (se2p_plan_probe_atomics).
 # * gather (k_gather_fix, int64 sums of exact products): bound by issue and
 #   load latency; work = warp instructions per target (ncu).
 # * filter: FP64 FLOP against cuBLAS DGEMM.
@@ -235,28 +235,6 @@ def reference_arm(args, rank, world):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def red_peak_gops(torch, dev):
-    """64-bit integer atomic adds to global memory per second, coalesced
-    (consecutive lanes on consecutive words, as the spread's stencil rows),
-    measured with torch's index_add_ over a 64 MB array (best of 5)."""
-    n, m = 2 ** 26, 2 ** 23
-    x = torch.zeros(m, dtype=torch.int64, device=dev)
-    idx = torch.arange(n, device=dev) % m
-    v = torch.ones(n, dtype=torch.int64, device=dev)
-    x.index_add_(0, idx, v)
-    torch.cuda.synchronize(dev)
-    best = 1e30
-    for _ in range(5):
-        s = torch.cuda.Event(enable_timing=True)
-        e = torch.cuda.Event(enable_timing=True)
-        s.record()
-        x.index_add_(0, idx, v)
-        e.record()
-        e.synchronize()
-        best = min(best, s.elapsed_time(e))
-    return n / (best * 1e-3) / 1e9
-
-
 def fp64_peak_tflops(torch, dev):
     """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
     n = 2048
@@ -579,6 +557,14 @@ def gpu_arm(args, rank, world, local_rank):
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     issue_peak = 4 * sms * clock_ghz * 1e9 / 1e12
     issue_src = "4 warp instructions per clock per SM x SMs x measured SM clock"
+    # the integer spread against the L2 atomic rate, whichever kernel is on top
+    spread_atomics = None
+    if "spread" in per:
+        red_peak = plan.probe_atomics()
+        red_done = N * SPREAD_RED_PER_SOURCE / (per["spread"] * 1e-3) / 1e9
+        spread_atomics = {"kernel": "k_spread_fix<5>", "achieved": red_done, "peak": red_peak,
+                          "unit": "G int64 atomics/s", "frac": red_done / red_peak,
+                          "ms_per_launch": per["spread"]}
     if top == "real":
         achieved = evals_per_launch * REAL_WARP_INST_PER_PAIR / (top_ms * 1e-3) / 1e12
         roof = {"kernel": "k_real<SLP,DLP,float-float> (fused real-space pair sum)",
@@ -591,8 +577,9 @@ def gpu_arm(args, rank, world, local_rank):
     elif top == "spread":
         roof = {"kernel": "k_spread_fix<5> (integer spread, 5 grids)", "bound": "l2_atomics",
                 "achieved": N * SPREAD_RED_PER_SOURCE / (top_ms * 1e-3) / 1e9,
-                "peak": red_peak_gops(torch, dev), "unit": "G int64 atomics/s",
-                "peak_source": "coalesced int64 index_add_ measured in this run "
+                "peak": spread_atomics["peak"], "unit": "G int64 atomics/s",
+                "peak_source": "coalesced 64-bit integer atomics into an L2-resident array, "
+                               "se2p_plan_probe_atomics in this run "
                                "(MEASURED_PEAKS.json holds no atomic figure)"}
     else:
         flops = M * (M // 2 + 1) * FILTER_FLOP_PER_MODE
@@ -603,6 +590,7 @@ def gpu_arm(args, rank, world, local_rank):
     roof.update({"frac": roof["achieved"] / roof["peak"],
                  "traffic": DRAM_BYTES.get(top), "traffic_unit": "bytes/launch (ncu)",
                  "ms_per_launch": top_ms, "top_stage": top,
+                 "spread_atomics": spread_atomics,
                  "real_space": {"ms_per_launch": per.get("real"),
                                 "accepted_pairs_per_launch": pairs_per_launch,
                                 "candidates_per_launch": counts[0] / n_serial,

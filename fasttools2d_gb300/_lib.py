@@ -25,6 +25,7 @@ EXPORTS = (
     "se2p_slp_real", "se2p_slp_kspace", "se2p_dlp_real", "se2p_dlp_kspace",
     "se2p_slp_ewald", "se2p_dlp_ewald", "se2p_stokes_ewald",
     "se2p_plan_enable_timing", "se2p_num_stages", "se2p_stage_name", "se2p_plan_stage_times",
+    "se2p_plan_probe_atomics",
     "se2p_plan_count_pairs", "se2p_slp_real_noalloc", "se2p_plan_set_precision",
     "se2p_plan_set_overlap", "se2p_stokes_ewald_adjoint",
     "se2p_geom_create", "se2p_geom_apply", "se2p_geom_bytes", "se2p_geom_pairs",
@@ -83,6 +84,7 @@ def load(path: str = LIB_PATH):
         L.se2p_plan_enable_timing.argtypes = [P, i32]
         L.se2p_stage_name.argtypes = [i32]
         L.se2p_stage_name.restype = ctypes.c_char_p
+        L.se2p_plan_probe_atomics.argtypes = [P, ctypes.POINTER(ctypes.c_double)]
         L.se2p_plan_stage_times.argtypes = [P, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_int64), i32]
         L.se2p_plan_count_pairs.argtypes = [P, i32, ctypes.POINTER(ctypes.c_int64), i32]
@@ -156,6 +158,12 @@ class Plan:
         calls = (ctypes.c_int64 * n)()
         self.check(self.lib.se2p_plan_stage_times(self.handle, ms, calls, 1 if reset else 0))
         return {self.lib.se2p_stage_name(i).decode(): (ms[i], calls[i]) for i in range(n)}
+
+    def probe_atomics(self) -> float:
+        """Coalesced 64-bit integer L2 atomics per second on this device, in G/s."""
+        g = ctypes.c_double()
+        self.check(self.lib.se2p_plan_probe_atomics(self.handle, ctypes.byref(g)))
+        return g.value
 
     def count_pairs(self, on: bool = True, reset: bool = True):
         """Turn the real-space counters on/off; returns (candidates, slp_pairs, dlp_pairs)."""

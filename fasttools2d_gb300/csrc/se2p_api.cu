@@ -46,6 +46,7 @@ enum Slot {
     S_TWY, S_TWX,                               // float-float FFT twiddles (y, x lengths)
     S_SPL, S_TPL,                               // low halves of sorted positions (FP32 grid)
     S_MTAB,                                     // cached per-mode filter multipliers
+    S_PROBE,                                    // the atomic-rate probe's array
     S_COUNT_SLOTS
 };
 
@@ -1503,6 +1504,38 @@ int se2p_plan_count_pairs(se2p_plan pl, int on, int64_t *counts, int reset)
 }
 
 const char *se2p_stage_name(int i) { return (i >= 0 && i < T_NUM_STAGES) ? kStageNames[i] : ""; }
+
+int se2p_plan_probe_atomics(se2p_plan pl, double *gops)
+{
+    if (!pl || !gops) return SE2P_ERR_ARG;
+    DeviceGuard guard(pl->device);
+    cudaStream_t st = pl->stream;
+    const int64_t n = (int64_t)1 << 22;              // 32 MB
+    unsigned long long *a = nullptr;
+    CKS(ensure_t(pl, S_PROBE, (size_t)n, &a));
+    CK(cudaMemsetAsync(a, 0, sizeof(unsigned long long) * (size_t)n, st));
+    int64_t count = 0;
+    CK(launch_probe_red64(a, n, 64, &count, st));    // warm-up
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    cudaError_t err = cudaSuccess;
+    for (int r = 0; r < 5 && err == cudaSuccess; r++) {
+        err = cudaEventRecord(e0, st);
+        if (err == cudaSuccess) err = launch_probe_red64(a, n, 1024, &count, st);
+        if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float t = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+        if (err == cudaSuccess && t > 0.f) best = std::min(best, t);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(err);
+    *gops = (double)count / (best * 1e-3) / 1e9;
+    return SE2P_OK;
+}
 
 int se2p_plan_stage_times(se2p_plan pl, double *ms, int64_t *calls, int reset)
 {

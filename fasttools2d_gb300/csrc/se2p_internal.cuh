@@ -457,6 +457,10 @@ cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &lau
 // With a.gff set (adj_gather_ff_ok), the float-float gather runs, and the
 // FP64 one only when the grid holds a non-finite value.
 bool adj_gather_ff_ok(double a, double h, double w, int P);
+// iters coalesced 64-bit atomic adds per thread into a[0..n) (n >= 256 x 8 x
+// SMs); *count = the atomics launched.
+cudaError_t launch_probe_red64(unsigned long long *a, int64_t n, int iters, int64_t *count,
+                               cudaStream_t st);
 cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches);
 cudaError_t launch_adj_assemble(int64_t n, const int *perm, const double *gr, const double *gk,
                                 const double *w, int64_t nt, double2 *part,

@@ -2977,6 +2977,30 @@ cudaError_t launch_filter_adj(const FilterArgs &a, cudaStream_t st, int64_t &lau
     return cudaGetLastError();
 }
 
+// Rate probe of the L2 atomic units: every thread adds 1 to `iters` words of
+// an n-word array small enough to stay in L2, lane l of a warp on word w + l
+// (the spread's stencil rows issue their 64-bit atomics the same way).
+__global__ void k_probe_red64(unsigned long long *__restrict__ a, int64_t n, int iters)
+{
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) % n;
+    for (int k = 0; k < iters; k++) {
+        atomicAdd(a + w, 1ull);
+        w += nth;
+        if (w >= n) w -= n;
+    }
+}
+
+cudaError_t launch_probe_red64(unsigned long long *a, int64_t n, int iters, int64_t *count,
+                               cudaStream_t st)
+{
+    const unsigned g = (unsigned)sm_count() * 8;
+    if ((int64_t)g * 256 > n) return cudaErrorInvalidValue;   // one wrap per step at most
+    k_probe_red64<<<g, 256, 0, st>>>(a, n, iters);
+    *count = (int64_t)g * 256 * iters;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_adj(const GatherAdjArgs &a, cudaStream_t st, int64_t &launches)
 {
     if (a.ns <= 0) return cudaSuccess;

@@ -108,6 +108,13 @@ int se2p_num_stages(void);
 const char *se2p_stage_name(int stage);
 int se2p_plan_stage_times(se2p_plan plan, double *ms, int64_t *calls, int reset);
 
+/* Measurement helper, no reference counterpart: the rate of coalesced 64-bit
+ * integer atomic adds into an L2-resident array on the plan's device, in G/s
+ * (best of 5 CUDA-event timings on the plan's stream; 32 MB of workspace).
+ * It is the denominator of the integer spread's roofline, which issues one
+ * such atomic per stencil node and grid. */
+int se2p_plan_probe_atomics(se2p_plan plan, double *gops);
+
 /* Real-space work counters: with counting on, the real-space kernel adds up
  * per call the candidate sources it examined and the SLP and DLP pairs it
  * accepted.  Sets counting on/off and returns the totals so far in
