@@ -248,7 +248,7 @@ struct RealWarp {
     double acc[kRing][4];       // per-target sums: SLP u1, u2, DLP u1, u2
     float2 accf[kRing][4];      // the same from float-float pairs (FP64 form, queue 0)
     double2 tpos[kRing];
-    int tbox[kRing];
+    int2 tbxy[kRing];           // the target's box as (column, row)
     long long tidx[kRing];
     long long tend[2][kRing];   // FIFO position after the target's last pair
     int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
@@ -315,8 +315,8 @@ __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, 
     const double2 S = a.sp[s];
     const double2 T = W.tpos[slot];
     // image shift of neighbour k: 0 or the reference's (L*(+-nside))/nside
-    const int tb = W.tbox[slot];
-    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const int2 tb = W.tbxy[slot];
+    const int ux = tb.x + c_nb_dx[k], uy = tb.y + c_nb_dy[k];
     // Without a periodic image both offset forms are exactly s - t; across an
     // image (rare) the SLP form s-(t-z) and the DLP form (s-t)+z are formed
     // separately and each kernel keeps its own r2, as the reference does.
@@ -410,8 +410,8 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
                                               float &d2)
 {
     const int s = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
-    const int tb = W.tbox[slot];
-    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const int2 tb = W.tbxy[slot];
+    const int ux = tb.x + c_nb_dx[k], uy = tb.y + c_nb_dy[k];
     // The offset s - t + z from float-float positions, on the FP32 pipe: the
     // TwoSum of the high halves is exact, the image shift z (zxf = (z-.hi,
     // z-.lo, z+.hi, z+.lo)) cancels its head exactly (Sterbenz: the two are
@@ -483,8 +483,8 @@ __device__ __forceinline__ void real_pair_ff(const RealArgs &a, const RealWarp &
     const double2 S = a.sp[s];
     const double2 T = W.tpos[slot];
     // image shift of neighbour k of this pair's target (the FIFO outlives W.nbz)
-    const int tb = W.tbox[slot];
-    const int ux = tb % a.nx + c_nb_dx[k], uy = tb / a.nx + c_nb_dy[k];
+    const int2 tb = W.tbxy[slot];
+    const int ux = tb.x + c_nb_dx[k], uy = tb.y + c_nb_dy[k];
     double dx = S.x - T.x, dy = S.y - T.y;
     if (ux < 0 || ux >= a.nx || uy < 0 || uy >= a.ny) {   // across a periodic image
         dx += ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         }
         if (lane == 0) {
             W.tpos[slot] = T;
-            W.tbox[slot] = tb;
+            W.tbxy[slot] = make_int2(tb % a.nx, tb / a.nx);
             W.tidx[slot] = t;
             if (MIXED) {
                 const float2 tl = a.tpl[t];
