@@ -835,7 +835,7 @@ struct AdjWarp {
     double acc[kRing][kAdjVals + 1];
     float2 accf[kRing][kAdjVals];    // the same from float-float pairs (FP64 form, queue 0)
     double2 pos[kRing];
-    int box[kRing];
+    int2 bxy[kRing];            // the source's box as (column, row)
     long long idx[kRing];
     long long tend[2][kRing];
     int nbs[9], nbp[10];
@@ -900,12 +900,14 @@ __device__ __forceinline__ void adj_pair(const RealArgs &a, const AdjWarp &W, in
     const int t = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
     const double2 T = a.tp[t];                  // forward target (inner point)
     const double2 S = W.pos[slot];              // forward source (outer point)
-    // image shift of the source seen from the target's box: unwrapped source
-    // box = target box - offset k
-    const int tbx = a.tbox[t] % a.nx, tby = a.tbox[t] / a.nx;
-    const int ux = tbx - c_nb_dx[k], uy = tby - c_nb_dy[k];
-    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    // image shift of the source seen from the target's box: the target sits
+    // in box wrap(source box + offset k), so the unwrapped source box
+    // (target box - offset k) lies below 0 exactly when source box + offset
+    // reached past the last box, and beyond it when that went below 0
+    const int2 b = W.bxy[slot];
+    const int tx = b.x + c_nb_dx[k], ty = b.y + c_nb_dy[k];
+    const double zx = tx >= a.nx ? a.zxm : (tx < 0 ? a.zxp : 0.0);
+    const double zy = ty >= a.ny ? a.zym : (ty < 0 ? a.zyp : 0.0);
     const double x1 = (S.x - T.x) + zx, x2 = (S.y - T.y) + zy;          // DLP form
     const double d1 = S.x - (T.x - zx), d2 = S.y - (T.y - zy);          // SLP form
     const double *wt = a.wcoef + 4 * (int64_t)t;                         // w_slp, w_dlp of t
@@ -980,10 +982,11 @@ __device__ __forceinline__ void adj_pair_ff(const RealArgs &a, const AdjWarp &W,
     const int t = e.x, slot = e.y & 0xff, k = (e.y >> 8) & 0xf, fl = e.y >> 12;
     const double2 T = a.tp[t];
     const double2 S = W.pos[slot];
-    const int tbx = a.tbox[t] % a.nx, tby = a.tbox[t] / a.nx;
-    const int ux = tbx - c_nb_dx[k], uy = tby - c_nb_dy[k];
-    const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-    const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+    // (the image shift as in adj_pair)
+    const int2 b = W.bxy[slot];
+    const int tx = b.x + c_nb_dx[k], ty = b.y + c_nb_dy[k];
+    const double zx = tx >= a.nx ? a.zxm : (tx < 0 ? a.zxp : 0.0);
+    const double zy = ty >= a.ny ? a.zym : (ty < 0 ? a.zyp : 0.0);
     const float2 x1 = ff_split((S.x - T.x) + zx), x2 = ff_split((S.y - T.y) + zy);
     const float2 r2 = ff_add(ff_sqr(x1), ff_sqr(x2));
     const float2 x = ff_mul(r2, xi2);
@@ -1170,7 +1173,7 @@ __global__ void __launch_bounds__(kAdjWarps * 32, 5) k_real_adj(RealArgs a)
         if (lane < kAdjVals) W.accf[slot][lane] = make_float2(0.f, 0.f);
         if (lane == 0) {
             W.pos[slot] = Sp;
-            W.box[slot] = sbx;
+            W.bxy[slot] = make_int2(sbx % a.nx, sbx / a.nx);
             W.idx[slot] = s;
         }
         int cntk = 0;
