@@ -73,6 +73,7 @@ struct se2p_plan_st {
     cudaStream_t side = nullptr;     // real space runs here, concurrently with k space
     cudaStream_t kst = nullptr;      // k space beside real space (highest priority)
     cudaEvent_t fork = nullptr, join = nullptr, kjoin = nullptr;
+    cudaEvent_t cin0 = nullptr, cin1 = nullptr;   // densities' host copies on the side stream
     std::string err;
     int64_t launches = 0;
     DevBuf buf[S_COUNT_SLOTS];
@@ -215,7 +216,7 @@ bool device_ready(const se2p_plan pl, const void *p)
 // Input array of `count` double2: use in place when it is usable device
 // memory, otherwise copy it into workspace slot `slot`.
 int stage_in(se2p_plan pl, int slot, const double *p, int64_t count, const double2 **out,
-             bool *host_io)
+             bool *host_io, cudaStream_t cs = nullptr)
 {
     *out = nullptr;
     if (count <= 0 || !p) return SE2P_OK;
@@ -225,7 +226,8 @@ int stage_in(se2p_plan pl, int slot, const double *p, int64_t count, const doubl
     }
     double2 *d = nullptr;
     CKS(ensure_t(pl, slot, (size_t)count, &d));
-    CK(cudaMemcpyAsync(d, p, sizeof(double2) * (size_t)count, cudaMemcpyDefault, pl->stream));
+    CK(cudaMemcpyAsync(d, p, sizeof(double2) * (size_t)count, cudaMemcpyDefault,
+                       cs ? cs : pl->stream));
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type != cudaMemoryTypeDevice &&
         at.type != cudaMemoryTypeManaged)
@@ -717,11 +719,18 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     StageTimer *t_in = new StageTimer(pl, T_STAGE_IN);
     CKS(stage_in(pl, S_IN_PS, io.psrc, ns, &ps, &host_io));
     CKS(stage_in(pl, S_IN_PT, io.ptar, nt, &pt, &host_io));
-    if (J.slp) CKS(stage_in(pl, S_IN_F, io.f_slp, ns, &fs, &host_io));
+    // Host densities and normals are copied on the side stream, beside the
+    // wrap and sort that need only the positions; the stream waits for
+    // everything queued before (the staging slots' last readers), and the
+    // coefficient kernel waits for the copies.
+    CK(cudaEventRecord(pl->cin0, st));
+    CK(cudaStreamWaitEvent(pl->side, pl->cin0, 0));
+    if (J.slp) CKS(stage_in(pl, S_IN_F, io.f_slp, ns, &fs, &host_io, pl->side));
     if (J.dlp) {
-        CKS(stage_in(pl, S_IN_FD, io.f_dlp, ns, &fd, &host_io));
-        CKS(stage_in(pl, S_IN_N, io.nrm, ns, &nr, &host_io));
+        CKS(stage_in(pl, S_IN_FD, io.f_dlp, ns, &fd, &host_io, pl->side));
+        CKS(stage_in(pl, S_IN_N, io.nrm, ns, &nr, &host_io, pl->side));
     }
+    CK(cudaEventRecord(pl->cin1, pl->side));
     OutBuf o_us, o_urs, o_uks, o_ud, o_urd, o_ukd;
     CKS(stage_out(pl, S_OUT0, io.u_slp, nt, &o_us, &host_io));
     CKS(stage_out(pl, S_OUT1, io.u_dlp, nt, &o_ud, &host_io));
@@ -731,7 +740,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     delete t_in;
     if (io.ur_slp && io.ur_dlp) return fail(pl, SE2P_ERR_ARG, "internal: both part outputs requested");
 
-    if (nt == 0) return SE2P_OK;
+    if (nt == 0) {
+        if (host_io) CK(cudaStreamSynchronize(pl->side));   // the copies read host memory
+        return SE2P_OK;
+    }
 
     // Wrapped positions (driver composites); the raw sources stay for the zero mode.
     const double2 *ws = ps, *wt = pt;
@@ -794,6 +806,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     const int doff = J.slp ? 2 : 0;
     double *coef = nullptr;
     CKS(ensure_t(pl, S_COEF, (size_t)nc * nsz, &coef));
+    CK(cudaStreamWaitEvent(st, pl->cin1, 0));        // the densities are in
     {
         StageTimer tm(pl, T_COEF);
         CK(launch_src_coef(ns, sperm, J.slp ? fs : nullptr, J.dlp ? fd : nullptr, nr, coef, nc, st,
@@ -1401,7 +1414,9 @@ int se2p_plan_create(se2p_plan *plan, int device)
         cudaStreamCreateWithPriority(&pl->kst, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&pl->kjoin, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&pl->kjoin, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->cin0, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->cin1, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         se2p_plan_destroy(pl);
         return SE2P_ERR_CUDA;
@@ -1436,6 +1451,8 @@ int se2p_plan_destroy(se2p_plan pl)
     if (pl->fork) cudaEventDestroy(pl->fork);
     if (pl->join) cudaEventDestroy(pl->join);
     if (pl->kjoin) cudaEventDestroy(pl->kjoin);
+    if (pl->cin0) cudaEventDestroy(pl->cin0);
+    if (pl->cin1) cudaEventDestroy(pl->cin1);
     if (pl->own) cudaStreamDestroy(pl->own);
     delete pl;
     return SE2P_OK;
