@@ -202,3 +202,21 @@ def test_fixed_forms_carry_non_finite_values(ft, plans):
          for pl in plans]
     assert not np.all(np.isfinite(a[1]))
     assert np.array_equal(np.isfinite(a[0]), np.isfinite(a[1]))
+
+
+def test_ff_adjoint_gather_hands_non_finite_grids_to_fp64(ft, plans):
+    """A NaN target weight makes the adjoint grids non-finite; the
+    float-float adjoint gather then steps aside and the FP64 one carries the
+    NaNs, so both forms' gradients are non-finite at the same places."""
+    ff, nat = plans
+    N = 5000
+    p, q, f, g, n = _cloud(N, 47)
+    rng = np.random.default_rng(48)
+    w1, w2 = rng.standard_normal((2, N)), rng.standard_normal((2, N))
+    w1[1, 123] = np.nan
+    prm = ft.EwaldParams.derived(60.0, 12, 12, 192, 192, 24, 1.0, 1.0)
+    a = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm, plan=ff)
+    b = ft.stokes_ewald_adjoint(p, q, f, g, n, w1, w2, prm, plan=nat)
+    assert not np.all(np.isfinite(b[0]))
+    for x, y in zip(a, b):
+        assert np.array_equal(np.isfinite(x), np.isfinite(y))
