@@ -110,23 +110,31 @@ def config(N, extra=None):
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+    """nvidia-smi samples (every 100 ms, time-stamped) while the context is
+    open; summary() keeps those inside the windows marked with window(), the
+    timed regions, with one sampling interval of slack."""
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    PERIOD_S = 0.1
 
     def __init__(self, gpu_id):
         self.gpu_id = gpu_id
         self.proc = None
+        self.windows = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu_id), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(int(self.PERIOD_S * 1000))],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
         return self
+
+    def window(self, t0, t1):
+        self.windows.append((t0, t1))
 
     def __exit__(self, *exc):
         self.rows = []
@@ -140,21 +148,30 @@ class ClockSampler:
             out, _ = self.proc.communicate()
         for line in out.splitlines():
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) == 7:
-                self.rows.append(parts)
+            if len(parts) == 8:
+                try:
+                    t = time.mktime(time.strptime(parts[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
+                    t += float("0." + parts[0].split(".")[1]) if "." in parts[0] else 0.0
+                except (ValueError, IndexError):
+                    t = None
+                self.rows.append((t, parts[1:]))
         return False
 
     def summary(self):
         if not getattr(self, "rows", None):
             return None
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        sl = self.PERIOD_S
+        inside = [r for t, r in self.rows if t is not None and
+                  any(t0 - sl <= t <= t1 + sl for t0, t1 in self.windows)]
+        rows = inside or [r for _, r in self.rows]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4)
+        reasons = sorted({names[i] for r in rows for i in range(4)
                           if r[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(rows), "in_timed_regions": bool(inside)}
 
 
 # ---------------------------------------------------------------------------
@@ -483,32 +500,38 @@ def gpu_arm(args, rank, world, local_rank):
     def max_over_ranks(x):
         return aggregate_replicas(x, 1, world, dev)[0]
 
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize(dev)
-
-    # ---- device-resident timed region (no stage events, no pair counters) --
-    launches0 = plan.kernel_launches
     gpu_id = local_rank
     try:
         gpu_id = str(torch.cuda.get_device_properties(dev).uuid)
         gpu_id = gpu_id if gpu_id.startswith("GPU-") else "GPU-" + gpu_id
     except Exception:
         pass
-    barrier()
+    # the clock sampler starts before the warm-up, so that it is sampling
+    # when the timed regions begin; it keeps the samples taken inside them
     with ClockSampler(gpu_id) as clk:
+        for _ in range(args.warmup):
+            step_device()
+        torch.cuda.synchronize(dev)
+
+        # ---- device-resident timed region (no stage events, no pair counters)
+        launches0 = plan.kernel_launches
+        barrier()
+        t0 = time.time()
         total_ms = timed(step_device, args.steps)
         barrier()
-    launches = plan.kernel_launches - launches0
-    total_ms, value = aggregate_replicas(total_ms, args.steps, world, dev)
-    ms_per_step = total_ms / args.steps
+        clk.window(t0, time.time())
+        launches = plan.kernel_launches - launches0
+        total_ms, value = aggregate_replicas(total_ms, args.steps, world, dev)
+        ms_per_step = total_ms / args.steps
 
-    # ---- end to end through the C ABI with pinned host buffers ------------
-    for _ in range(max(1, args.warmup // 2)):
-        step_host()
-    barrier()
-    e2e_ms = max_over_ranks(timed(step_host, args.steps))
-    barrier()
+        # ---- end to end through the C ABI with pinned host buffers --------
+        for _ in range(max(1, args.warmup // 2)):
+            step_host()
+        barrier()
+        t0 = time.time()
+        e2e_ms = max_over_ranks(timed(step_host, args.steps))
+        barrier()
+        clk.window(t0, time.time())
     e2e = {"value": world * args.steps / (e2e_ms * 1e-3), "unit": UNIT,
            "h2d_bytes_per_step": 5 * N * 16, "d2h_bytes_per_step": 2 * N * 16,
            "ms_per_step": e2e_ms / args.steps}
