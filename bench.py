@@ -629,6 +629,8 @@ def gpu_arm(args, rank, world, local_rank):
         "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
         "clocks": clk.summary(), "fp32_grid": mixed, "adjoint": adjoint,
         "multi_rhs": multi,
+        # the metric's secondary unit: targets evaluated per second (N_t / t)
+        "target_evals_per_s": value * N,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N)
