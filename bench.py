@@ -212,14 +212,20 @@ def cpu_threads():
     return O.num_threads()
 
 
-def cpu_baseline(N):
+def cpu_baseline(N, reps=5):
+    """The oracle port on the host cores: the median of `reps` full
+    evaluations after one warm-up (about 10 s at N = 2^20)."""
     run, kind = cpu_eval_fn(N, prefer_reference=False)
-    t0 = time.perf_counter()
     run()
-    dt = time.perf_counter() - t0
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        run()
+        ts.append(time.perf_counter() - t0)
+    dt = statistics.median(ts)
     return {"value": 1.0 / dt, "unit": UNIT, "cores": cpu_threads(), "kind": kind,
-            "sample": f"one full SLP+DLP evaluation at N={N} (oracle C restatement, OpenMP, "
-                      f"scipy FFT), {dt:.2f} s"}
+            "sample": f"median of {reps} full SLP+DLP evaluations at N={N} after one warm-up "
+                      f"(oracle C restatement, OpenMP, scipy FFT), {dt:.2f} s each"}
 
 
 def reference_arm(args, rank, world):
