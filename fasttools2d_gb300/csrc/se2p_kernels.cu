@@ -306,6 +306,30 @@ __device__ __forceinline__ void seg_flush_ff(RealWarp &W, int lane, int key, flo
     __syncwarp();
 }
 
+// seg_flush for the FP32-grid form's float sums: the tree adds in float
+// (the lanes' own sums are float already), and each segment's total joins
+// the slot's float-float accumulator.
+__device__ __forceinline__ void seg_flush_f(RealWarp &W, int lane, int key, float v0, float v1,
+                                            float v2, float v3)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ko = __shfl_up_sync(~0u, key, o);
+        const float a0 = __shfl_up_sync(~0u, v0, o), a1 = __shfl_up_sync(~0u, v1, o);
+        const float a2 = __shfl_up_sync(~0u, v2, o), a3 = __shfl_up_sync(~0u, v3, o);
+        if (lane >= o && ko == key) {
+            v0 += a0; v1 += a1; v2 += a2; v3 += a3;
+        }
+    }
+    const int kn = __shfl_down_sync(~0u, key, 1);
+    if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
+        float2 *a = W.accf[key % kRing];
+        a[0] = ff_add_f(a[0], v0); a[1] = ff_add_f(a[1], v1);
+        a[2] = ff_add_f(a[2], v2); a[3] = ff_add_f(a[3], v3);
+    }
+    __syncwarp();
+}
+
 template <bool SLP, bool DLP>
 __device__ __forceinline__ void real_pair(const RealArgs &a, const RealWarp &W, int2 e,
                                           const double *tab, const double *e1s, double &s1,
@@ -591,9 +615,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
                 seg_flush_ff(W, lane, P.tag, fl ? P.h1 : z, fl ? P.h2 : z, fl ? P.k1 : z,
                              fl ? P.k2 : z);
             } else if (f32) {
-                seg_flush_ff(W, lane, P.tag, make_float2(fl ? P.f1 : 0.f, 0.f),
-                             make_float2(fl ? P.f2 : 0.f, 0.f), make_float2(fl ? P.g1 : 0.f, 0.f),
-                             make_float2(fl ? P.g2 : 0.f, 0.f));
+                seg_flush_f(W, lane, P.tag, fl ? P.f1 : 0.f, fl ? P.f2 : 0.f, fl ? P.g1 : 0.f,
+                            fl ? P.g2 : 0.f);
             } else {
                 seg_flush(W, lane, P.tag, fl ? P.s1 : 0.0, fl ? P.s2 : 0.0, fl ? P.d1 : 0.0,
                           fl ? P.d2 : 0.0);
@@ -635,8 +658,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
             batch(j, Q[j].qn);
             const int key = Q[j].tag >= 0 ? Q[j].tag : 0x7fffffff;
             if (MIXED && j == 0)
-                seg_flush_ff(W, lane, key, make_float2(Q[j].f1, 0.f), make_float2(Q[j].f2, 0.f),
-                             make_float2(Q[j].g1, 0.f), make_float2(Q[j].g2, 0.f));
+                seg_flush_f(W, lane, key, Q[j].f1, Q[j].f2, Q[j].g1, Q[j].g2);
             else if (FF && j == 0)
                 seg_flush_ff(W, lane, key, Q[j].h1, Q[j].h2, Q[j].k1, Q[j].k2);
             else
