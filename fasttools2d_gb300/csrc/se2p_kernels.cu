@@ -282,26 +282,36 @@ __device__ __forceinline__ void seg_flush(RealWarp &W, int lane, int key, double
 }
 
 // seg_flush for float-float sums (queue 0 of the FP64 form), into W.accf.
+// The tree adds the heads with TwoSum and carries tails and TwoSum errors
+// in the second float unnormalised; each segment's total is normalised once
+// before it joins the slot's accumulator.
 __device__ __forceinline__ void seg_flush_ff(RealWarp &W, int lane, int key, float2 v0, float2 v1,
                                              float2 v2, float2 v3)
 {
+    float2 v[4] = {v0, v1, v2, v3};
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int ko = __shfl_up_sync(~0u, key, o);
-        float2 a0, a1, a2, a3;
-        a0.x = __shfl_up_sync(~0u, v0.x, o); a0.y = __shfl_up_sync(~0u, v0.y, o);
-        a1.x = __shfl_up_sync(~0u, v1.x, o); a1.y = __shfl_up_sync(~0u, v1.y, o);
-        a2.x = __shfl_up_sync(~0u, v2.x, o); a2.y = __shfl_up_sync(~0u, v2.y, o);
-        a3.x = __shfl_up_sync(~0u, v3.x, o); a3.y = __shfl_up_sync(~0u, v3.y, o);
+        float2 a[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            a[k].x = __shfl_up_sync(~0u, v[k].x, o);
+            a[k].y = __shfl_up_sync(~0u, v[k].y, o);
+        }
         if (lane >= o && ko == key) {
-            v0 = ff_add(v0, a0); v1 = ff_add(v1, a1); v2 = ff_add(v2, a2); v3 = ff_add(v3, a3);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                float s, e;
+                two_sum(v[k].x, a[k].x, s, e);
+                v[k] = make_float2(s, v[k].y + a[k].y + e);
+            }
         }
     }
     const int kn = __shfl_down_sync(~0u, key, 1);
     if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
-        float2 *a = W.accf[key % kRing];
-        a[0] = ff_add(a[0], v0); a[1] = ff_add(a[1], v1);
-        a[2] = ff_add(a[2], v2); a[3] = ff_add(a[3], v3);
+        float2 *acc = W.accf[key % kRing];
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[k] = ff_add(acc[k], ff_norm(v[k].x, v[k].y));
     }
     __syncwarp();
 }
