@@ -912,15 +912,20 @@ __device__ __forceinline__ void seg_flush_n_ff(Acc &accs, int lane, int key, flo
             a[i].y = __shfl_up_sync(~0u, v[i].y, o);
         }
         if (lane >= o && ko == key) {
+            // heads by TwoSum, tails and errors carried unnormalised (as in seg_flush_ff)
 #pragma unroll
-            for (int i = 0; i < NV; i++) v[i] = ff_add(v[i], a[i]);
+            for (int i = 0; i < NV; i++) {
+                float s, e;
+                two_sum(v[i].x, a[i].x, s, e);
+                v[i] = make_float2(s, v[i].y + a[i].y + e);
+            }
         }
     }
     const int kn = __shfl_down_sync(~0u, key, 1);
     if (key >= 0 && key != 0x7fffffff && (lane == 31 || kn != key)) {
         float2 *a = accs[key % kRing];
 #pragma unroll
-        for (int i = 0; i < NV; i++) a[i] = ff_add(a[i], v[i]);
+        for (int i = 0; i < NV; i++) a[i] = ff_add(a[i], ff_norm(v[i].x, v[i].y));
     }
     __syncwarp();
 }
