@@ -74,7 +74,7 @@ UNIT = "evals/s"
 C_IN, C_OUT = 5, 4
 SPREAD_RED_PER_SOURCE = (P + 1) ** 2 * C_IN
 FILTER_FLOP_PER_MODE = 60
-DRAM_BYTES = {"spread": 2.008e9, "gather": 0.279e9, "real": 0.267e9}
+DRAM_BYTES = {"spread": 2.008e9, "gather": 0.279e9, "real": 0.182e9}
 REAL_WARP_INST_PER_PAIR = 42.7     # ncu smsp__inst_executed / SLP+DLP pair evaluations
 GATHER_WARP_INST_PER_TARGET = 1508.0   # ncu smsp__inst_executed / targets (k_gather_fix<4,24>)
 
