@@ -17,10 +17,17 @@ Printed JSON line:
   e2e           evals/s through the C ABI with pinned HOST buffers, the
                 host->device copies of the inputs and device->host copies of
                 both outputs inside the timed region
-  roofline      dominant kernel: executed FP64 FLOP/s against the FP64 peak
-                measured in this run (cuBLAS DGEMM), plus its HBM side
+  roofline      dominant kernel: its arithmetic work per launch over its
+                CUDA-event time against the peak of the pipe that bounds it
+                (real space: FP32 thread instructions of the float-float pair
+                evaluations against 128 lanes x SMs x SM clock), plus its
+                HBM side against the measured copy bandwidth
   cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP path)
-                on this host's cores, one full evaluation
+                on this host's cores, median of full evaluations
+  parity_vs_oracle  the end-to-end outputs against the oracle's on the same
+                inputs, per potential: normwise, RMS-relative and the
+                99.9-percentile of the pointwise relative error
+  fp64_native   the all-FP64 form on the same workload (rate and parity)
   gpu_launches  this library's kernel launches in the timed region
   clocks        nvidia-smi samples taken during the timed region
 
@@ -60,8 +67,11 @@ METRIC = "SE Stokes evals/s @1M pts: FP64 tol 1e-10 vs FP32-grid tol 1e-6; fwd+a
 UNIT = "evals/s"
 # Roofline inputs of the library's own kernels on this workload (FP64 form).
 # * real space (k_real, far pairs in float-float on the FP32 pipe): bound by
-#   instruction issue; work = warp instructions per accepted pair evaluation
-#   (ncu smsp__inst_executed / evaluations).
+#   the FP32 pipe; work = the FP32 thread instructions (FADD + FFMA + FMUL,
+#   ncu) of one SLP+DLP pair evaluation, times the accepted pairs counted in
+#   this run; peak = 128 FP32 lanes x SMs x the SM clock sampled in this run.
+#   Issue utilisation (warp instructions per evaluation, ncu) is reported
+#   beside it.
 # * spread (k_spread_fix, exact int64 sums): bound by L2 atomics; work = one
 #   64-bit reduction per stencil node and grid, (P+1)^2 C_in per source with
 #   C_in = 5 grids (SLP f1, f2; DLP S11, S12+S21, S22); peak = coalesced int64
@@ -76,7 +86,14 @@ SPREAD_RED_PER_SOURCE = (P + 1) ** 2 * C_IN
 FILTER_FLOP_PER_MODE = 60
 DRAM_BYTES = {"spread": 2.008e9, "gather": 0.279e9, "real": 0.182e9}
 REAL_WARP_INST_PER_PAIR = 42.7     # ncu smsp__inst_executed / SLP+DLP pair evaluations
+REAL_FP32_INST_PER_EVAL = 542.0    # ncu FADD 360 + FFMA 125 + FMUL 57 thread instructions per evaluation
 GATHER_WARP_INST_PER_TARGET = 1508.0   # ncu smsp__inst_executed / targets (k_gather_fix<4,24>)
+# Algorithmic HBM bytes of one launch, each array read or written once:
+# real space reads per sorted source its position (16 B), FP32 copy (8 B), 5
+# FP64 coefficients and 7 float-float ones (96 B), and per target its
+# position, FP32 copy and box (28 B), and writes 2 x 16 B of sums.
+REAL_ALG_BYTES_PER_POINT = (16 + 8 + 96, 16 + 8 + 4 + 32)   # (per source, per target)
+FALLBACK_HBM_GBS = 6800.0
 
 
 def workload(N):
@@ -104,6 +121,32 @@ def config(N, extra=None):
     if extra:
         c.update(extra)
     return c
+
+
+def err_stats(a, b):
+    """Error of a against b, both (N, 2): normwise max|a-b| / max|b|, RMS-relative
+    ||a-b|| / ||b||, and the 99.9-percentile over targets of the pointwise
+    relative error |a_t - b_t| / |b_t| (2-norms per target)."""
+    a = np.asarray(a, dtype=np.float64).reshape(-1, 2)
+    b = np.asarray(b, dtype=np.float64).reshape(-1, 2)
+    ok = np.isfinite(b).all(axis=1) & np.isfinite(a).all(axis=1)
+    a, b = a[ok], b[ok]
+    d = a - b
+    nb = np.hypot(b[:, 0], b[:, 1])
+    pw = np.hypot(d[:, 0], d[:, 1]) / np.where(nb > 0, nb, np.inf)
+    return {"max_rel": float(np.abs(d).max() / np.abs(b).max()),
+            "rms_rel": float(np.sqrt(np.mean(d * d) / np.mean(b * b))),
+            "p999_rel": float(np.quantile(pw, 0.999)),
+            "nonfinite_mismatch": int((~ok).sum())}
+
+
+def measured_hbm_gbs():
+    """(GB/s, source): the copy bandwidth in MEASURED_PEAKS.json, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError, KeyError):
+        return FALLBACK_HBM_GBS, "fallback (one earlier GB300 measurement)"
 
 
 # ---------------------------------------------------------------------------
@@ -202,8 +245,10 @@ def cpu_eval_fn(N, prefer_reference):
             return run, kind
 
     def run():
-        O.slp_ewald(S, T, F, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)
-        O.dlp_ewald(S, T, G, Nn, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)
+        """(u_slp, u_dlp) as (N, 2) arrays."""
+        us = O.slp_ewald(S, T, F, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)[0]
+        ud = O.dlp_ewald(S, T, G, Nn, prm.xi, prm.nside_x, prm.nside_y, M, M, L, L, P)[0]
+        return us.T, ud.T
     return run, kind
 
 
@@ -214,9 +259,11 @@ def cpu_threads():
 
 def cpu_baseline(N, reps=5):
     """The oracle port on the host cores: the median of `reps` full
-    evaluations after one warm-up (about 10 s at N = 2^20)."""
+    evaluations after one warm-up (about 10 s at N = 2^20).  Returns the
+    baseline record and the oracle's outputs (u_slp, u_dlp), which the GPU
+    results are checked against."""
     run, kind = cpu_eval_fn(N, prefer_reference=False)
-    run()
+    out = run()
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -225,7 +272,7 @@ def cpu_baseline(N, reps=5):
     dt = statistics.median(ts)
     return {"value": 1.0 / dt, "unit": UNIT, "cores": cpu_threads(), "kind": kind,
             "sample": f"median of {reps} full SLP+DLP evaluations at N={N} after one warm-up "
-                      f"(oracle C restatement, OpenMP, scipy FFT), {dt:.2f} s each"}
+                      f"(oracle C restatement, OpenMP, scipy FFT), {dt:.2f} s each"}, out
 
 
 def reference_arm(args, rank, world):
@@ -281,16 +328,25 @@ def fp64_peak_tflops(torch, dev):
 XI4, RC4, M4, P4 = 860.0, 0.0042, 2048, 12
 
 
-def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
-    """FP32-grid vs FP64 on the mixed-precision workload: evals/s of each, speed-up, and the
-    FP32-grid error against the FP64 result per potential (max, RMS)."""
+# ncu dram__bytes_read + _write of one launch of the FP32-grid k-space kernels
+# at the mixed-precision workload (profiles/), None until captured.
+F32_DRAM_BYTES = {"spread": None, "gather": None}
+
+
+def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev, with_oracle):
+    """FP32-grid vs FP64 on the mixed-precision workload: evals/s of each, speed-up, the
+    FP32-grid error against the FP64 result and (with_oracle) against the CPU oracle run
+    on the same points and parameters, per potential; and the HBM roofline of the
+    FP32-grid spread and gather from a serialised pass with stage timing."""
     import torch
     import fasttools2d_gb300 as ft
     nside = int(math.floor(L / RC4))
-    prm4 = ft.EwaldParams.derived(XI4, nside, nside, M4, M4, P4, L, L).as_c()
+    prm4p = ft.EwaldParams.derived(XI4, nside, nside, M4, M4, P4, L, L)
+    prm4 = prm4p.as_c()
     L_ = plan.lib
     out = {}
     res = {}
+    stages = None
     for prec in ("fp64", "fp32_grid"):
         plan.set_precision(prec)
         u = [torch.empty_like(u_dev[0]), torch.empty_like(u_dev[1])]
@@ -305,23 +361,93 @@ def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev):
         ms = timed(step, steps) / steps
         res[prec] = [x.double().cpu().numpy() for x in u]
         out[prec] = {"evals_per_s": 1e3 / ms, "ms_per_step": ms}
+        if prec == "fp32_grid":
+            plan.set_overlap(False)
+            plan.enable_timing(True)
+            plan.stage_times(reset=True)
+            for _ in range(2):
+                step()
+            torch.cuda.synchronize(dev)
+            stages = plan.stage_times(reset=True)
+            plan.enable_timing(False)
+            plan.set_overlap(True)
     plan.set_precision("fp64")
-    err = {}
-    for i, name in enumerate(("slp", "dlp")):
-        a, b = res["fp32_grid"][i], res["fp64"][i]
-        err[name] = {"max_rel": float(np.abs(a - b).max() / np.abs(b).max()),
-                     "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))}
-    return {"workload": f"SE SLP+DLP, same 1M points, xi={XI4}, rc={RC4} (nside={nside}), M={M4}, "
+    err = {name: err_stats(res["fp32_grid"][i], res["fp64"][i])
+           for i, name in enumerate(("slp", "dlp"))}
+    line = {"workload": f"SE SLP+DLP, same 1M points, xi={XI4}, rc={RC4} (nside={nside}), M={M4}, "
                         f"P={P4}, tol 1e-6",
             "value": out["fp32_grid"]["evals_per_s"], "unit": UNIT,
             "ms_per_step": out["fp32_grid"]["ms_per_step"],
             "fp64_same_workload": out["fp64"],
             "speedup_vs_fp64_same_workload": out["fp32_grid"]["evals_per_s"] / out["fp64"]["evals_per_s"],
             "error_vs_fp64": err}
+    if with_oracle:
+        from oracle import oracle as O
+        psrc, ptar, f, g, n = workload(N)
+        S, T = psrc.T.copy(), ptar.T.copy()
+        ros = O.slp_ewald(S, T, f.T.copy(), XI4, nside, nside, M4, M4, L, L, P4)[0].T
+        rod = O.dlp_ewald(S, T, g.T.copy(), n.T.copy(), XI4, nside, nside, M4, M4, L, L, P4)[0].T
+        line["error_vs_oracle"] = {"fp32_grid": {"slp": err_stats(res["fp32_grid"][0], ros),
+                                                 "dlp": err_stats(res["fp32_grid"][1], rod)},
+                                   "fp64": {"slp": err_stats(res["fp64"][0], ros),
+                                            "dlp": err_stats(res["fp64"][1], rod)},
+                                   "oracle": "CPU oracle (FP64) on the same points and parameters"}
+    # HBM roofline of the FP32-grid k-space kernels (serialised stage times):
+    # the spread reads per source its position and 5 FP64 coefficients (56 B)
+    # and writes the 5 FP32 grids once; the gather reads per target its
+    # position (16 B), the 4 FP32 grids once, and writes 2 x 16 B.
+    hbm, hbm_src = measured_hbm_gbs()
+    G4 = M4 * M4
+    alg = {"spread": N * 56 + G4 * 5 * 4, "gather": N * (16 + 32) + G4 * 4 * 4}
+    roof = {}
+    for k in ("spread", "gather"):
+        if stages and k in stages and stages[k][1] > 0:
+            ms = stages[k][0] / stages[k][1]
+            gbs = alg[k] / (ms * 1e-3) / 1e9
+            roof[k] = {"kernel": f"k_{k}_f32", "bound": "hbm", "ms_per_launch": ms,
+                       "alg_bytes": alg[k], "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                       "frac": gbs / hbm, "peak_source": hbm_src,
+                       "traffic": F32_DRAM_BYTES[k], "traffic_unit": "bytes/launch (ncu)"}
+    line["roofline"] = roof
+    line["stage_ms"] = {k: round(v[0] / max(1, v[1]), 4) for k, v in (stages or {}).items()
+                        if v[1] > 0}
+    return line
+
+
+def native_leg(plan, tens, u_dev, N, steps, timed, oracle_out):
+    """The all-FP64 form (every floating-point step an FP64 instruction, as the
+    reference computes it) on the headline workload: its rate, and its parity
+    with the oracle when the oracle's outputs are at hand."""
+    import torch
+    L_ = plan.lib
+    cprm = params(N).as_c()
+    u = [torch.empty_like(u_dev[0]), torch.empty_like(u_dev[1])]
+    plan.set_precision("fp64_native")
+
+    def step():
+        plan.check(L_.se2p_stokes_ewald(plan.handle, ctypes.byref(cprm), tens[0].data_ptr(), N,
+                                        tens[1].data_ptr(), N, tens[2].data_ptr(),
+                                        tens[3].data_ptr(), tens[4].data_ptr(),
+                                        u[0].data_ptr(), u[1].data_ptr()))
+    try:
+        for _ in range(2):
+            step()
+        k = max(2, steps // 2)
+        ms = timed(step, k) / k
+    finally:
+        plan.set_precision("fp64")
+    line = {"workload": "the headline workload, precision SE2P_PRECISION_FP64_NATIVE",
+            "evals_per_s": 1e3 / ms, "ms_per_step": ms, "steps": k}
+    if oracle_out is not None:
+        got = [x.cpu().numpy() for x in u]
+        line["parity_vs_oracle"] = {"slp": err_stats(got[0], oracle_out[0]),
+                                    "dlp": err_stats(got[1], oracle_out[1])}
+    return line
 
 
 # The adjoint workload: forward + adjoint, N = 2^18.
 N5, XI5, RC5, M5, P5 = 2 ** 18, 430.0, 0.011, 1344, 24
+FD_COORDS = 64
 
 
 def multi_rhs_leg(plan, tens, N, ms_single, dev, nrhs=4):
@@ -367,7 +493,7 @@ def adjoint_leg(plan, steps, timed, dev):
     """Adjoint workload: time of the forward and of forward + adjoint (gradients of
     J = sum_t w_slp.u_slp + w_dlp.u_dlp w.r.t. source positions, forces,
     densities, normals), and a central-difference check of the gradients on
-    16 random coordinates (h = 1e-6, J from the GPU forward)."""
+    64 random coordinates (h = 1e-6, J from the GPU forward)."""
     import torch
     import fasttools2d_gb300 as ft
     rng = np.random.default_rng(20261203 + 5)
@@ -405,7 +531,7 @@ def adjoint_leg(plan, steps, timed, dev):
         both()
     t_f = timed(fwd, steps) / steps
     t_fa = timed(both, steps) / steps
-    # finite differences on 16 coordinates: positions, forces, densities, normals
+    # finite differences on 64 coordinates: positions, forces, densities, normals
     both()
     torch.cuda.synchronize(dev)
     G = [x.cpu().numpy() for x in g]
@@ -417,7 +543,7 @@ def adjoint_leg(plan, steps, timed, dev):
     def J():
         fwd()
         return float((Wt[0] * u[0]).sum() + (Wt[1] * u[1]).sum())
-    for _ in range(16):
+    for _ in range(FD_COORDS):
         a = int(pick.choice([0, 2, 3, 4]))
         i, k = int(pick.integers(0, N)), int(pick.integers(0, 2))
         x0 = float(T[a][i, k])
@@ -431,7 +557,7 @@ def adjoint_leg(plan, steps, timed, dev):
     return {"workload": f"SE SLP+DLP forward+adjoint, N={N} sources + {N} targets uniform, xi={XI5}, rc={RC5} "
                         f"(nside={nside}), M={M5}, P={P5}, FP64; J = sum_t w.u with w ~ N(0,1)",
             "fwd_ms": t_f, "fwd_adjoint_ms": t_fa, "ratio_fwd_adjoint_over_fwd": t_fa / t_f,
-            "fd_check": {"coords": 16, "h": h, "max_err_rel_to_max_grad": worst}}
+            "fd_check": {"coords": FD_COORDS, "h": h, "max_err_rel_to_max_grad": worst}}
 
 
 def aggregate_replicas(local_ms, steps, world, device=None):
@@ -560,9 +686,26 @@ def gpu_arm(args, rank, world, local_rank):
     plan.enable_timing(False)
     plan.set_overlap(True)
 
-    # ---- FP32-grid form (mixed-precision workload) next to the FP64 form on the same workload
+    # ---- the oracle on the same inputs: CPU baseline and parity ----------
     legs = set(args.legs.split(","))
-    mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev) \
+    cpu = oracle_out = parity = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, oracle_out = cpu_baseline(N)
+        got = [x.numpy() for x in u_host]               # the end-to-end (host) outputs
+        dev_out = [x.cpu().numpy() for x in u_dev]       # the device-resident outputs
+        parity = {"slp": err_stats(got[0], oracle_out[0]), "dlp": err_stats(got[1], oracle_out[1]),
+                  "device_vs_host_outputs": max(err_stats(dev_out[i], got[i])["max_rel"]
+                                                for i in range(2)),
+                  "oracle": "CPU oracle (FP64 restatement of the reference) on the same inputs",
+                  "bar": "normwise and RMS-relative <= 1e-12 per potential"}
+
+    # ---- the all-FP64 form on the same workload ---------------------------
+    native = native_leg(plan, tens, u_dev, N, args.steps, timed, oracle_out) \
+        if "fp64_native" in legs else None
+
+    # ---- FP32-grid form (mixed-precision workload) next to the FP64 form on the same workload
+    mixed = mixed_precision_leg(plan, tens, u_dev, N, args.steps, timed, dev,
+                                with_oracle=oracle_out is not None) \
         if "fp32_grid" in legs else None
     if mixed is not None:
         # the metric's own pairing: FP32-grid at tolerance 1e-6 against the
@@ -586,6 +729,8 @@ def gpu_arm(args, rank, world, local_rank):
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     issue_peak = 4 * sms * clock_ghz * 1e9 / 1e12
     issue_src = "4 warp instructions per clock per SM x SMs x measured SM clock"
+    fp32_peak = 128 * sms * clock_ghz * 1e9 / 1e12
+    hbm, hbm_src = measured_hbm_gbs()
     # the integer spread against the L2 atomic rate, whichever kernel is on top
     spread_atomics = None
     if "spread" in per:
@@ -593,12 +738,38 @@ def gpu_arm(args, rank, world, local_rank):
         red_done = N * SPREAD_RED_PER_SOURCE / (per["spread"] * 1e-3) / 1e9
         spread_atomics = {"kernel": "k_spread_fix<5>", "achieved": red_done, "peak": red_peak,
                           "unit": "G int64 atomics/s", "frac": red_done / red_peak,
-                          "ms_per_launch": per["spread"]}
+                          "ms_per_launch": per["spread"],
+                          "hbm_side": {"traffic": DRAM_BYTES["spread"],
+                                       "alg_bytes": N * (16 + 8 * C_IN) + M * M * C_IN * 8}}
+    real_side = None
+    if "real" in per:
+        rms_ = per["real"]
+        alg = N * (REAL_ALG_BYTES_PER_POINT[0] + REAL_ALG_BYTES_PER_POINT[1])
+        real_side = {
+            "kernel": "k_real<SLP,DLP,float-float>", "ms_per_launch": rms_,
+            "accepted_pairs_per_launch": pairs_per_launch,
+            "evaluations_per_launch": evals_per_launch,
+            "candidates_per_launch": counts[0] / n_serial,
+            "candidates_per_evaluation": counts[0] / n_serial / max(1.0, evals_per_launch),
+            "pairs_per_s": pairs_per_launch / (rms_ * 1e-3),
+            "fp32_pipe": {"achieved": evals_per_launch * REAL_FP32_INST_PER_EVAL / (rms_ * 1e-3) / 1e12,
+                          "peak": fp32_peak, "unit": "T FP32 thread-inst/s",
+                          "work_per_evaluation": REAL_FP32_INST_PER_EVAL,
+                          "peak_source": "128 FP32 lanes per SM x SMs x measured SM clock"},
+            "issue": {"achieved": evals_per_launch * REAL_WARP_INST_PER_PAIR / (rms_ * 1e-3) / 1e12,
+                      "peak": issue_peak, "unit": "T warp-inst/s",
+                      "work_per_evaluation": REAL_WARP_INST_PER_PAIR, "peak_source": issue_src},
+            "hbm_side": {"alg_bytes": alg, "achieved": alg / (rms_ * 1e-3) / 1e9, "peak": hbm,
+                         "unit": "GB/s", "traffic": DRAM_BYTES["real"]}}
+        for k in ("fp32_pipe", "issue", "hbm_side"):
+            real_side[k]["frac"] = real_side[k]["achieved"] / real_side[k]["peak"]
     if top == "real":
-        achieved = evals_per_launch * REAL_WARP_INST_PER_PAIR / (top_ms * 1e-3) / 1e12
         roof = {"kernel": "k_real<SLP,DLP,float-float> (fused real-space pair sum)",
-                "bound": "issue", "achieved": achieved, "peak": issue_peak,
-                "unit": "T warp-inst/s", "peak_source": issue_src}
+                "bound": "fp32", "achieved": real_side["fp32_pipe"]["achieved"],
+                "peak": fp32_peak, "unit": "T FP32 thread-inst/s",
+                "peak_source": real_side["fp32_pipe"]["peak_source"],
+                "work": f"{REAL_FP32_INST_PER_EVAL:.0f} FP32 thread instructions (FADD+FFMA+FMUL, ncu) "
+                        "per SLP+DLP pair evaluation x evaluations counted in this run"}
     elif top == "gather":
         roof = {"kernel": "k_gather_fix<4,24> (integer gather, 4 grids)", "bound": "issue",
                 "achieved": N * GATHER_WARP_INST_PER_TARGET / (top_ms * 1e-3) / 1e12,
@@ -619,12 +790,7 @@ def gpu_arm(args, rank, world, local_rank):
     roof.update({"frac": roof["achieved"] / roof["peak"],
                  "traffic": DRAM_BYTES.get(top), "traffic_unit": "bytes/launch (ncu)",
                  "ms_per_launch": top_ms, "top_stage": top,
-                 "spread_atomics": spread_atomics,
-                 "real_space": {"ms_per_launch": per.get("real"),
-                                "accepted_pairs_per_launch": pairs_per_launch,
-                                "candidates_per_launch": counts[0] / n_serial,
-                                "pairs_per_s": pairs_per_launch / (per["real"] * 1e-3)
-                                if "real" in per else None}})
+                 "spread_atomics": spread_atomics, "real_space": real_side})
     stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1] > 0}
 
     line = {
@@ -633,13 +799,13 @@ def gpu_arm(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config(N, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
         "e2e": e2e, "roofline": roof, "gpu_launches": launches, "stage_ms": stage_ms,
-        "clocks": clk.summary(), "fp32_grid": mixed, "adjoint": adjoint,
-        "multi_rhs": multi,
+        "clocks": clk.summary(), "parity_vs_oracle": parity, "fp64_native": native,
+        "fp32_grid": mixed, "adjoint": adjoint, "multi_rhs": multi,
         # the metric's secondary unit: targets evaluated per second (N_t / t)
         "target_evals_per_s": value * N,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(N)
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
     plan.close()
@@ -653,11 +819,20 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="points (sources = targets count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--legs", default="fp32_grid,adjoint,multi_rhs",
-                    help="extra legs after the headline workload: fp32_grid, adjoint, multi_rhs, "
-                         "or none "
+    ap.add_argument("--legs", default="fp64_native,fp32_grid,adjoint,multi_rhs",
+                    help="extra legs after the headline workload: fp64_native, fp32_grid, adjoint, "
+                         "multi_rhs, or none "
                          "(a profiling run of the headline workload alone uses none)")
+    ap.add_argument("--shrink", type=int, default=1, choices=[1, 4, 16],
+                    help="profiling cases: N / shrink points with xi, 1/rc and M divided by "
+                         "sqrt(shrink), so the points per box and per grid node stay the same "
+                         "(4: 2^18 points, xi=430, nside=89, M=1344)")
     args = ap.parse_args()
+    if args.shrink > 1:
+        global XI, RC, M
+        r = int(round(math.sqrt(args.shrink)))
+        XI, RC, M = XI / r, RC * r, M // r
+        args.n //= args.shrink
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

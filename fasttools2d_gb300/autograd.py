@@ -3,8 +3,11 @@
 A thin ``torch.autograd.Function`` over se2p_stokes_ewald (forward) and
 se2p_stokes_ewald_adjoint (backward), used to check the hand-written adjoint
 kernels against finite differences.  Tensors are (N, 2) float64 on the GPU;
-gradients flow to the source positions, SLP forces, DLP densities and normals
-(not to the target positions).
+gradients flow to the source positions, SLP forces, DLP densities and normals.
+The target positions take no gradient: a ptar that requires one (for
+instance the source positions passed again as targets, the usual
+boundary-integral self-evaluation) raises, since its part of the gradient
+would otherwise be missing without notice.
 """
 from __future__ import annotations
 
@@ -16,6 +19,11 @@ from .ewald import EwaldParams, stokes_ewald, stokes_ewald_adjoint
 class StokesEwald(torch.autograd.Function):
     @staticmethod
     def forward(ctx, psrc, ptar, f_slp, f_dlp, n, prm: EwaldParams, plan):
+        if ctx.needs_input_grad[1]:
+            raise NotImplementedError(
+                "stokes_ewald_torch: gradients with respect to the target positions are not "
+                "implemented; pass ptar.detach() (when ptar is psrc, the gradient would lack "
+                "the target-position part)")
         u_slp, u_dlp = stokes_ewald(psrc, ptar, f_slp, f_dlp, n, prm, plan=plan)
         ctx.save_for_backward(psrc, ptar, f_slp, f_dlp, n)
         ctx.prm, ctx.plan = prm, plan

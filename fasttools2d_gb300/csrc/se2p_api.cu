@@ -741,7 +741,10 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     if (io.ur_slp && io.ur_dlp) return fail(pl, SE2P_ERR_ARG, "internal: both part outputs requested");
 
     if (nt == 0) {
-        if (host_io) CK(cudaStreamSynchronize(pl->side));   // the copies read host memory
+        // The staging copies on the side stream read the caller's inputs:
+        // the caller's stream waits for them, and host inputs are waited for.
+        CK(cudaStreamWaitEvent(st, pl->cin1, 0));
+        if (host_io) CK(cudaStreamSynchronize(pl->side));
         return SE2P_OK;
     }
 
@@ -817,7 +820,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
     if (J.real) {
         if (J.slp) CKS(ensure_t(pl, S_UR_SLP, ntz, &ur_slp));
         if (J.dlp) CKS(ensure_t(pl, S_UR_DLP, ntz, &ur_dlp));
-        RealArgs ra;
+        RealArgs ra{};
         ra.sp = sp;
         ra.spf = spf;
         ra.tpf = tpf;
@@ -1206,7 +1209,7 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     CKS(ensure_t(pl, S_GK, 7 * nsz, &gk));
 
     // real space (side stream) ...
-    RealArgs ra;
+    RealArgs ra{};
     memset(&ra, 0, sizeof ra);
     ra.sp = sp;
     ra.spf = spf;
@@ -2047,16 +2050,19 @@ int se2p_stokes_ewald_adjoint(se2p_plan pl, const se2p_params *prm, const double
 // For callers that cannot call cudaMalloc (MATLAB MEX code whose GPU memory
 // belongs to gpuArray's allocator; solver loops that must not allocate).  The
 // working arrays of one call are carved from this fixed device array, which
-// each GPU that loads the library keeps until exit.  In host code the name
-// g_noalloc_scratch is only a host-side stand-in: its device address comes
-// from cudaGetSymbolAddress, once per device, with that device current.
+// each GPU that loads the library keeps until exit.  In host code the names
+// g_noalloc_scratch and g_noalloc_gtab are only host-side stand-ins: their
+// device addresses come from cudaGetSymbolAddress, looked up on every call
+// with the caller's device current (a host-side lookup), so that a context
+// created anew -- after cudaDeviceReset, or MATLAB's reset(gpuDevice) -- is
+// served with its own addresses.
 // ============================================================================
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SE2P_NOALLOC_SCRATCH_BYTES];
+// The E1 fit of the float-float pairs (the table gtab_device gives a plan),
+// copied in on every call from the process's host copy.
+static __device__ __align__(256) float4 g_noalloc_gtab[kGPieces * 3];
 
 namespace {
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[256] = {nullptr};
-
 size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 
 // Bytes of scratch one call needs (the carve order of se2p_slp_real_noalloc).
@@ -2065,7 +2071,7 @@ size_t noalloc_bytes(int64_t ns, int64_t nt, int64_t nbox)
     const size_t s = (size_t)(ns > 0 ? ns : 1), t = (size_t)nt, b = (size_t)nbox;
     return round256(4 * s) * 3 + round256(4 * t) * 4 + round256(4 * b) + 2 * round256(4 * (b + 1)) +
            round256(16 * s) + round256(16 * t) + round256(8 * s) + round256(8 * t) +
-           round256(16 * s) + round256(16 * t);
+           round256(16 * s) + round256(16 * t) + round256(16 * s);
 }
 
 bool on_device(const void *p, int dev)
@@ -2094,26 +2100,28 @@ extern "C" int se2p_slp_real_noalloc(const double *psrc, int64_t ns, const doubl
         noalloc_bytes(ns, nt, nbox) > SE2P_NOALLOC_SCRATCH_BYTES)
         return SE2P_ERR_UNSUPPORTED;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return SE2P_ERR_CUDA;
     }
     if (!ptar || !u || !on_device(ptar, dev) || !on_device(u, dev)) return SE2P_ERR_ARG;
     if (ns > 0 && (!psrc || !f || !on_device(psrc, dev) || !on_device(f, dev))) return SE2P_ERR_ARG;
+    const GFit &fit = gfit();
+    if (!(fit.worst < 1e-14)) return SE2P_ERR_UNSUPPORTED;
 
-    unsigned char *base;
-    {
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-                cudaGetLastError();
-                return SE2P_ERR_CUDA;
-            }
-            g_noalloc_addr[dev] = p;
-        }
-        base = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+    // Device addresses of the two file-scope arrays in the current context.
+    void *sp_base = nullptr, *gt = nullptr;
+    if (cudaGetSymbolAddress(&sp_base, g_noalloc_scratch) != cudaSuccess || !sp_base ||
+        cudaGetSymbolAddress(&gt, g_noalloc_gtab) != cudaSuccess || !gt) {
+        cudaGetLastError();
+        return SE2P_ERR_CUDA;
     }
+    unsigned char *base = static_cast<unsigned char *>(sp_base);
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    if (cudaMemcpyAsync(gt, fit.tab.data(), fit.tab.size() * sizeof(float), cudaMemcpyHostToDevice,
+                        st) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+
     const size_t s1 = (size_t)(ns > 0 ? ns : 1), t1 = (size_t)nt;
     size_t off = 0;
     auto carve = [&](size_t bytes) {
@@ -2130,8 +2138,8 @@ extern "C" int se2p_slp_real_noalloc(const double *psrc, int64_t ns, const doubl
     float2 *spf = (float2 *)carve(8 * s1), *tpf = (float2 *)carve(8 * t1);
     double *coef = (double *)carve(16 * s1);
     double2 *ur = (double2 *)carve(16 * t1);
+    float2 *coef_ff = (float2 *)carve(16 * s1);
 
-    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     int64_t launches = 0;
     const double2 *ps = reinterpret_cast<const double2 *>(psrc);
     const double2 *pt = reinterpret_cast<const double2 *>(ptar);
@@ -2144,7 +2152,11 @@ extern "C" int se2p_slp_real_noalloc(const double *psrc, int64_t ns, const doubl
     if (launch_src_coef(ns, sperm, reinterpret_cast<const double2 *>(f), nullptr, nullptr, coef,
                         2, st, launches) != cudaSuccess)
         return SE2P_ERR_CUDA;
-    RealArgs ra;
+    if (launch_src_coef_ff(ns, coef, 2, true, false, coef_ff, 2, st, launches) != cudaSuccess)
+        return SE2P_ERR_CUDA;
+    // The same real-space arguments and form as se2p_slp_real on a plan of
+    // the default precision (SE2P_PRECISION_FP64: far pairs in float-float).
+    RealArgs ra{};
     ra.sp = sp;
     ra.spf = spf;
     ra.tpf = tpf;
@@ -2174,7 +2186,11 @@ extern "C" int se2p_slp_real_noalloc(const double *psrc, int64_t ns, const doubl
     ra.u_slp = ur;
     ra.u_dlp = nullptr;
     ra.counters = nullptr;
-    if (launch_real(ra, true, false, st, launches) != cudaSuccess) return SE2P_ERR_CUDA;
+    ra.coef_ff = coef_ff;
+    ra.ncf = 2;
+    ra.doff_ff = 0;
+    ra.gtab = static_cast<const float4 *>(gt);
+    if (launch_real(ra, true, false, st, launches, kFormFF) != cudaSuccess) return SE2P_ERR_CUDA;
     if (launch_assemble(nt, 0, tperm, ur, nullptr, nullptr, reinterpret_cast<double2 *>(u), nullptr,
                         nullptr, st, launches) != cudaSuccess)
         return SE2P_ERR_CUDA;

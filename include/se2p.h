@@ -72,16 +72,23 @@ int64_t se2p_plan_kernel_launches(se2p_plan plan);
 const char *se2p_version(void);
 
 /* ---- precision ----------------------------------------------------------------
- * SE2P_PRECISION_FP64 (default): FP64 inputs, outputs, grids and k-space
- * arithmetic; results within <= 1e-12 of the reference.  The far real-space
- * pairs (1 < xi^2 r^2 < 64) are evaluated in float-float arithmetic -- pairs
- * of FP32 values carrying about 48 bits -- because GB300 issues FP32 some 70
- * times faster than FP64; the real-space sum is well conditioned, so this
- * moves results by ~1e-15.  Near pairs, the SLP self term and the k-space
- * chain (spread, FFT, filter, gather, whose DLP part amplifies rounding
- * ~1000-fold) stay FP64.
+ * SE2P_PRECISION_FP64 (default): FP64 inputs and outputs, results within
+ * 1e-12 of the reference (normwise and RMS-relative, per potential).  Each
+ * stage runs in the narrowest arithmetic that keeps that bound, because GB300
+ * issues FP32 some 70 times faster than FP64:
+ *   - real space: the far pairs (1 < xi^2 r^2 < 64) in float-float arithmetic
+ *     (pairs of FP32 values carrying about 48 bits); near pairs, the SLP self
+ *     term and the exact cutoff decisions in FP64;
+ *   - spread and gather: exact integer arithmetic -- every Gaussian factor
+ *     rounded once to 62 bits, products as the high words of 64 x 64-bit
+ *     integer products rounded to nearest, sums as exact int64 additions (the
+ *     spread grid is bitwise reproducible); crowded grids or non-finite
+ *     values fall back to the FP64 spread and gather;
+ *   - FFT: float-float mixed-radix row transforms (cuFFT Z2Z for lengths with
+ *     prime factors above 7);
+ *   - filter, DLP k=0 term and the final sums: FP64.
  * SE2P_PRECISION_FP64_NATIVE: every floating-point step an FP64 instruction,
- * as the reference computes it.
+ * as the reference computes it (FP64 atomics, cuFFT Z2Z).
  * SE2P_PRECISION_FP32_GRID: the mixed form for tolerances >= 1e-6 --
  * spreading, FFT, filter and gather in FP32 and the far real-space pairs
  * (xi^2 r^2 > 1) in FP32, while the near real-space pairs (E1 at small
@@ -219,20 +226,26 @@ int se2p_geom_destroy(se2p_geom geom);
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: a MEX function running inside MATLAB, where gpuArray's caching
  * allocator owns the GPU's memory, or a solver's time-step loop that must not
- * stall or fail on cudaMalloc.  Computes exactly what se2p_slp_real computes,
- * but all working arrays live in one fixed file-scope device array of
- * SE2P_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU which loads this library
- * holds until the process exits; nothing is allocated or freed per call.
+ * stall or fail on cudaMalloc.  Computes what se2p_slp_real computes on a
+ * plan of the default precision (SE2P_PRECISION_FP64: far pairs in
+ * float-float, near pairs and the self term in FP64), but all working arrays
+ * live in one fixed file-scope device array of SE2P_NOALLOC_SCRATCH_BYTES
+ * (32 MiB), beside an 18 KB table of the E1 fit, which every GPU that loads
+ * this library holds until the process exits; nothing is allocated or freed
+ * per call.
  *
  *  - psrc, ptar, f and u must be device memory of the current device,
  *    16-byte aligned; the work is queued on `cuda_stream` (NULL = legacy
  *    default stream) and the call returns without synchronising.
  *  - Size limit: 256-byte-rounded arrays totalling about
- *    52*nsrc + 56*ntar + 12*nside_x*nside_y bytes must fit in 32 MiB
- *    (e.g. 290,000 sources plus 290,000 targets with nside 178); larger
+ *    68*nsrc + 56*ntar + 12*nside_x*nside_y bytes must fit in 32 MiB
+ *    (e.g. 265,000 sources plus 265,000 targets with nside 178); larger
  *    calls return SE2P_ERR_UNSUPPORTED before touching the GPU.
- *  - The first call on each device resolves the array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
+ *  - Every call looks the arrays' device addresses up (cudaGetSymbolAddress,
+ *    a host-side lookup) with the current device's context, and copies the
+ *    E1 table in from host memory on `cuda_stream`.  A context created anew
+ *    (after cudaDeviceReset, or MATLAB's reset(gpuDevice)) thus gets its own
+ *    arrays; the first call in a context also loads the module, so make it
  *    before any stream capture.
  *  - Every call reuses the same array, which keeps the previous call's
  *    contents (the per-box counters are cleared on each call); calls whose

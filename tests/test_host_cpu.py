@@ -97,3 +97,14 @@ def test_select_params_compat_switch():
         c = select_params(kind, 4000, 4000, 3e3, 1.0, Ly, tol=1e-10, compat=True)
         d = select_params(kind, 4000, 4000, 3e3, 1.0, Ly, tol=1e-10, compat=False)
         assert c.xi == d.xi and c.Mx > d.Mx
+
+
+def test_autograd_rejects_target_position_gradients():
+    """ptar requiring a gradient (e.g. psrc passed again as the targets) raises
+    before any GPU work, instead of returning a gradient without its
+    target-position part."""
+    torch = pytest.importorskip("torch")
+    from fasttools2d_gb300.autograd import stokes_ewald_torch
+    p = torch.zeros((4, 2), dtype=torch.float64, requires_grad=True)
+    with pytest.raises(NotImplementedError):
+        stokes_ewald_torch(p, p, p, p, p, None)
