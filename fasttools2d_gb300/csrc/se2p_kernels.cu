@@ -249,9 +249,11 @@ struct RealWarp {
     float2 accf[kRing][4];      // the same from float-float pairs (FP64 form, queue 0)
     double2 tpos[kRing];
     int2 tbxy[kRing];           // the target's box as (column, row)
-    long long tidx[kRing];
-    long long tend[2][kRing];   // FIFO position after the target's last pair
+    int tidx[kRing];
+    unsigned tend[2][kRing];    // FIFO position after the target's last pair (mod 2^32)
     int nbs[9], nbp[10];        // neighbour box: first sorted source, list prefix
+    int curbox;                 // the box those describe (-1: none yet)
+    int2 curbxy;                // and its (column, row)
     double2 nbz[9];
     float2 nbzf[9];
     float2 nbe[9];              // 2^-22 (|t| + |z|) per neighbour box (the pre-test band)
@@ -554,15 +556,18 @@ __device__ __forceinline__ void real_pair_ff(const RealArgs &a, const RealWarp &
 // Lane-side state of one pair FIFO.
 struct PairQueue {
     int qn;               // entries queued (warp-uniform)
-    long long enq, proc;  // entries enqueued / processed so far (warp-uniform)
+    unsigned enq, proc;   // entries enqueued / processed so far, mod 2^32 (warp-uniform)
     int tag;              // sequence number of the target this lane's sums belong to
     double s1, s2, d1, d2;
     float f1, f2, g1, g2; // FP32 sums of the mixed-precision form
     float2 h1, h2, k1, k2; // float-float sums of the FP64 form's far pairs
 };
 
+#ifndef SE2P_REAL_MINB
+#define SE2P_REAL_MINB 6
+#endif
 template <bool SLP, bool DLP, int FORM>
-__global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
+__global__ void __launch_bounds__(kRealWarps * 32, SE2P_REAL_MINB) k_real(RealArgs a)
 {
     constexpr bool MIXED = FORM == kFormF32;
     constexpr bool FF = FORM == kFormFF;
@@ -592,7 +597,6 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
     }
     __syncthreads();
     RealWarp &W = warps[wid];
-    const int64_t nw = (int64_t)gridDim.x * kRealWarps;
 
     int head = 0, nfl = 0, gseq = 0;   // ring head slot, targets in flight, targets started
     PairQueue Q[2];
@@ -603,7 +607,6 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         Q[j].f1 = Q[j].f2 = Q[j].g1 = Q[j].g2 = 0.f;
         Q[j].h1 = Q[j].h2 = Q[j].k1 = Q[j].k2 = make_float2(0.f, 0.f);
     }
-    unsigned long long ncand = 0, nslp = 0, ndlp = 0;
 
     // Evaluate the first cnt pairs of FIFO j (lanes >= cnt idle); lanes whose
     // sums belong to another target flush first.
@@ -648,10 +651,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
     };
     // Retire finished targets in order (all of them after a full flush).
     auto retire = [&](bool all) {
-        while (nfl > 0 && (all || (Q[0].proc >= W.tend[0][head] + 32 &&
-                                   Q[1].proc >= W.tend[1][head] + 32))) {
+        while (nfl > 0 && (all || ((int)(Q[0].proc - W.tend[0][head]) >= 32 &&
+                                   (int)(Q[1].proc - W.tend[1][head]) >= 32))) {
             if (lane < 4 && (lane < 2 ? SLP : DLP)) {
-                const long long t = W.tidx[head];
+                const int64_t t = W.tidx[head];
                 double v = W.acc[head][lane];
                 if (FF || MIXED) v += ff_to_double(W.accf[head][lane]);
                 double *u = reinterpret_cast<double *>(lane < 2 ? a.u_slp : a.u_dlp);
@@ -681,7 +684,16 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         retire(true);
     };
 
-    for (int64_t t = (int64_t)blockIdx.x * kRealWarps + wid; t < a.ntar; t += nw) {
+    // Each block takes one contiguous run of the box-sorted targets, and its
+    // warps interleave over it: a warp's consecutive targets mostly share a
+    // box (so its neighbour-box set is built once per box), and the block's
+    // warps read the same sources at the same time.
+    // (the cell lists hold int indices, so ntar < 2^31)
+    const int per = (int)((a.ntar + gridDim.x - 1) / gridDim.x);
+    const int t_end = (int)min(a.ntar, (int64_t)blockIdx.x * per + per);
+    if (lane == 0) W.curbox = -1;
+    __syncwarp();
+    for (int t = (int)blockIdx.x * per + wid; t < t_end; t += kRealWarps) {
         if (nfl == kRing) drain();
         const int slot = (head + nfl) % kRing;
         nfl++;
@@ -689,13 +701,23 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         const int tb = a.tbox[t];
         const double2 T = a.tp[t];
         const float2 Tf = a.tpf[t];
+        const bool newbox = tb != W.curbox;                // (warp-uniform)
+        if (newbox) {
+            __syncwarp();
+            if (lane == 0) {
+                W.curbox = tb;
+                W.curbxy = make_int2(tb % a.nx, tb / a.nx);
+            }
+            __syncwarp();
+        }
+        const int2 cur_bxy = W.curbxy;
         if (lane < 4) {
             W.acc[slot][lane] = 0.0;
             W.accf[slot][lane] = make_float2(0.f, 0.f);
         }
         if (lane == 0) {
             W.tpos[slot] = T;
-            W.tbxy[slot] = make_int2(tb % a.nx, tb / a.nx);
+            W.tbxy[slot] = cur_bxy;
             W.tidx[slot] = t;
             if (MIXED) {
                 const float2 tl = a.tpl[t];
@@ -703,33 +725,39 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
             }
         }
         // neighbour boxes: first source, counts -> list prefix, image shift
-        int cntk = 0;
-        if (lane < 9) {
-            const int ux = tb % a.nx + c_nb_dx[lane], uy = tb / a.nx + c_nb_dy[lane];
-            const int wx = (ux + a.nx) % a.nx, wy = (uy + a.ny) % a.ny;
-            const int sb = wy * a.nx + wx;
-            const int b0 = a.sstart[sb];
-            cntk = a.sstart[sb + 1] - b0;
-            W.nbs[lane] = b0;
-            const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
-            const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
-            W.nbz[lane] = make_double2(zx, zy);
-            const float zxf = (float)zx, zyf = (float)zy;
-            W.nbzf[lane] = make_float2(zxf, zyf);
-            W.nbe[lane] = make_float2(0x1p-22f * (fabsf(Tf.x) + fabsf(zxf)),
-                                      0x1p-22f * (fabsf(Tf.y) + fabsf(zyf)));
-        }
-        int incl = cntk;
+        // (once per box), and the pre-test band, which depends on the target
+        if (newbox) {
+            int cntk = 0;
+            if (lane < 9) {
+                const int ux = cur_bxy.x + c_nb_dx[lane], uy = cur_bxy.y + c_nb_dy[lane];
+                const int wx = (ux + a.nx) % a.nx, wy = (uy + a.ny) % a.ny;
+                const int sb = wy * a.nx + wx;
+                const int b0 = a.sstart[sb];
+                cntk = a.sstart[sb + 1] - b0;
+                W.nbs[lane] = b0;
+                const double zx = ux < 0 ? a.zxm : (ux >= a.nx ? a.zxp : 0.0);
+                const double zy = uy < 0 ? a.zym : (uy >= a.ny ? a.zyp : 0.0);
+                W.nbz[lane] = make_double2(zx, zy);
+                W.nbzf[lane] = make_float2((float)zx, (float)zy);
+            }
+            int incl = cntk;
 #pragma unroll
-        for (int o = 1; o < 16; o <<= 1) {
-            const int v = __shfl_up_sync(~0u, incl, o);
-            if (lane >= o) incl += v;
+            for (int o = 1; o < 16; o <<= 1) {
+                const int v = __shfl_up_sync(~0u, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane < 9) W.nbp[lane + 1] = incl;
+            if (lane == 0) W.nbp[0] = 0;
+            __syncwarp();
         }
-        if (lane < 9) W.nbp[lane + 1] = incl;
-        if (lane == 0) W.nbp[0] = 0;
+        if (lane < 9) {
+            const float2 zf = W.nbzf[lane];
+            W.nbe[lane] = make_float2(0x1p-22f * (fabsf(Tf.x) + fabsf(zf.x)),
+                                      0x1p-22f * (fabsf(Tf.y) + fabsf(zf.y)));
+        }
         __syncwarp();
         const int total = W.nbp[9];
-        ncand += (unsigned)total;
+        unsigned nslp = 0, ndlp = 0;
         int kc = 0;   // neighbour box of this lane's candidate (v only grows)
         for (int v0 = 0; v0 < total; v0 += 32) {
             const int v = v0 + lane;
@@ -821,16 +849,16 @@ __global__ void __launch_bounds__(kRealWarps * 32, 6) k_real(RealArgs a)
         if (lane == 0) {
             W.tend[0][slot] = Q[0].enq;
             W.tend[1][slot] = Q[1].enq;
+            if (a.counters) {                        // (diagnostic counts, per target)
+                atomicAdd(a.counters, (unsigned long long)total);
+                if (SLP) atomicAdd(a.counters + 1, (unsigned long long)nslp);
+                if (DLP) atomicAdd(a.counters + 2, (unsigned long long)ndlp);
+            }
         }
         __syncwarp();
         retire(false);
     }
     drain();
-    if (a.counters && lane == 0) {
-        atomicAdd(a.counters, ncand);
-        if (SLP) atomicAdd(a.counters + 1, nslp);
-        if (DLP) atomicAdd(a.counters + 2, ndlp);
-    }
 }
 
 template __global__ void k_real<true, false, kFormFP64>(RealArgs);
@@ -2869,7 +2897,7 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
     // (high-priority stream) takes what is left.  With 8-warp blocks at 94
     // registers only 16 warps fitted: 19.9 ms per evaluation at 2^20 points,
     // against 18.6 with 20 warps and 18.45 with 24.
-    const int64_t cap = (int64_t)sm_count() * 6;
+    const int64_t cap = (int64_t)sm_count() * SE2P_REAL_MINB;
     const unsigned g = (unsigned)(want < cap ? want : cap);
     if (form == kFormF32) launch_real_form<kFormF32>(a, slp, dlp, g, st);
     else if (form == kFormFF) launch_real_form<kFormFF>(a, slp, dlp, g, st);
