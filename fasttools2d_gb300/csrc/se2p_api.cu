@@ -47,6 +47,7 @@ enum Slot {
     S_SPL, S_TPL,                               // low halves of sorted positions (FP32 grid)
     S_MTAB,                                     // cached per-mode filter multipliers
     S_PROBE,                                    // the atomic-rate probe's array
+    S_MGRID, S_MGMAX, S_MUK, S_MZM,             // k space of several right-hand sides
     S_COUNT_SLOTS
 };
 
@@ -1881,6 +1882,171 @@ static int geom_build(se2p_geom g, const double *psrc, const double *ptar, const
     return SE2P_OK;
 }
 
+// Whether the k space of a geometry's right-hand sides can run batched
+// (geom_kspace_multi): the FP64 form with the integer spread and gather and
+// the float-float FFT.
+static bool geom_multi_ok(se2p_geom g, int *kY_out, double *kfac_out, int *mult_out)
+{
+    se2p_plan pl = g->pl;
+    const se2p_params &p = g->prm;
+    if (pl->precision != SE2P_PRECISION_FP64 || !fft_ff_ok(p.Mx, p.My)) return false;
+    SpreadArgs sa;
+    sa.Mx = p.Mx;
+    sa.My = p.My;
+    sa.P = p.P;
+    sa.h = p.Lx / p.Mx;
+    sa.w = p.w;
+    sa.a = -2 * p.xi * p.xi / p.eta;
+    int kY = 0, mult = 1;
+    double kfac = 1.0;
+    if (!spread_fixed_ok(sa, kY, kfac, mult) || kY != 0) return false;
+    *kY_out = kY;
+    *kfac_out = kfac;
+    *mult_out = mult;
+    return true;
+}
+
+// The k space of nr right-hand sides on a geometry's sorted points, in the
+// FP64 form (geom_multi_ok): coef holds nr blocks of nc coefficients per
+// sorted source (stride cstride doubles); uk receives per right-hand side r
+// the gathered sums at uk + r (nout / 2) nt, kind after kind, sorted target
+// order.  One spread launch covers all nr right-hand sides (each source's
+// stencil origin and Gaussian factors formed once), then each one's forward
+// transforms, filter and inverse transforms run into its own grids, and one
+// gather launch covers them all (each target's factors formed once).  A
+// right-hand side whose sources crowd too much for the integer sums, or whose
+// values are not finite, takes the FP64 spread or gather as in run().
+static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cstride,
+                             cudaStream_t ks, double2 *uk)
+{
+    se2p_plan pl = g->pl;
+    const se2p_params &p = g->prm;
+    const int Mx = p.Mx, My = p.My, P = p.P;
+    const size_t G = (size_t)Mx * My;
+    const int nc = (g->slp ? 2 : 0) + (g->dlp ? 3 : 0);
+    const int nout = (g->slp ? 2 : 0) + (g->dlp ? 2 : 0);
+    const double h = p.Lx / Mx;
+    int kY = 0, mult = 1;
+    double kfac = 1.0;
+    if (!geom_multi_ok(g, &kY, &kfac, &mult))
+        return fail(pl, SE2P_ERR_UNSUPPORTED, "internal: batched k space");
+    double *grid = nullptr, *e1 = nullptr, *ws = nullptr;
+    cufftDoubleComplex *spec = nullptr, *zg = nullptr;
+    unsigned long long *gmax = nullptr;
+    CKS(ensure_t(pl, S_MGRID, G * nc * (size_t)nr, &grid));
+    CKS(ensure_t(pl, S_SPEC, (size_t)Mx * (My / 2 + 1) * nc, &spec));
+    CKS(ensure_t(pl, S_ZGRID, G * (size_t)((nc + 1) / 2), &zg));
+    CKS(ensure_t(pl, S_E1, (size_t)P + 1, &e1));
+    CKS(ensure_t(pl, S_MGMAX, (size_t)nr, &gmax));
+    const int64_t nbin = (int64_t)spread_bins(Mx, P) * spread_bins(My, P);
+    const int64_t bstride = 2 * nbin + 1;
+    CKS(ensure_t(pl, S_SBINS, (size_t)bstride * nr, &ws));
+    // e1[j] = exp(-2 xi^2/eta h^2 j^2) (mex_stokes_slp_kspace.cpp:64-67)
+    double e1h[kMaxP + 1];
+    const double t = -2 * p.xi * p.xi / p.eta * h * h;
+    for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
+    CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, ks));
+    CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * nc * nr, ks));
+    CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long) * nr, ks));
+
+    SpreadArgs sa;
+    sa.sp = g->sp;
+    sa.coef = coef;
+    sa.ns = g->ns;
+    sa.grid = grid;
+    sa.Mx = Mx;
+    sa.My = My;
+    sa.P = P;
+    sa.Lhx = p.Lx / 2.0;
+    sa.Lhy = p.Ly / 2.0;
+    sa.h = h;
+    sa.w = p.w;
+    sa.a = -2 * p.xi * p.xi / p.eta;
+    sa.e1 = e1;
+    auto rhs_spread = [&](int r) {
+        SpreadArgs sr = sa;
+        sr.coef = coef + r * cstride;
+        sr.grid = grid + (size_t)r * nc * G;
+        sr.bound = reinterpret_cast<const unsigned long long *>(ws + r * bstride + nbin);
+        return sr;
+    };
+    {
+        StageTimer tm(pl, T_SPREAD, ks);
+        for (int r = 0; r < nr; r++)
+            CK(launch_spread_bound(rhs_spread(r), nc, kfac, mult, ws + r * bstride, ks, pl->launches));
+        sa.bound = reinterpret_cast<const unsigned long long *>(ws + nbin);
+        CK(launch_spread_fix_multi(sa, nc, kY, nr, cstride, (int64_t)(nc * G), (int)bstride, ks,
+                                   pl->launches));
+        for (int r = 0; r < nr; r++)                 // (the FP64 spread: returns at once unless crowded)
+            CK(launch_spread(rhs_spread(r), nc, ks, pl->launches));
+    }
+    const int Bg = gather_fixed_bits(sa);
+    FilterArgs fa;
+    fa.spec = spec;
+    fa.Mx = Mx;
+    fa.My = My;
+    fa.Lx = p.Lx;
+    fa.Ly = p.Ly;
+    fa.xi = p.xi;
+    fa.eta = p.eta;
+    fa.scale = 1.0 / ((double)Mx * (double)My);
+    fa.slp_in = g->slp ? 0 : -1;
+    fa.dlp_in = g->dlp ? (g->slp ? 2 : 0) : -1;
+    fa.slp_out = 0;
+    fa.dlp_out = g->slp ? 2 : 0;
+    fa.transposed = 1;
+    for (int r = 0; r < nr; r++) {
+        double *gr = grid + (size_t)r * nc * G;
+        const auto *fixb = reinterpret_cast<const unsigned long long *>(ws + r * bstride + nbin);
+        {
+            StageTimer tm(pl, T_FFT_FWD, ks);
+            CKS(fft_fwd_1d(pl, ks, Mx, My, gr, nc, zg, spec, fixb, true));
+        }
+        {
+            StageTimer tm(pl, T_FILTER, ks);
+            CKS(filter_matrix(pl, fa, ks));
+            CK(launch_filter(fa, ks, pl->launches));
+        }
+        {
+            StageTimer tm(pl, T_FFT_INV, ks);
+            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, gr, true, gmax + r));
+        }
+    }
+    GatherArgs ga;
+    ga.tp = g->tp;
+    ga.nt = g->nt;
+    ga.grid = grid;
+    ga.Mx = Mx;
+    ga.My = My;
+    ga.P = P;
+    ga.Lhx = p.Lx / 2.0;
+    ga.Lhy = p.Ly / 2.0;
+    ga.h = h;
+    ga.w = p.w;
+    ga.a = -2 * p.xi * p.xi / p.eta;
+    double sc = 4 * p.xi * p.xi / p.eta;             // mex_stokes_slp_kspace.cpp:325-328
+    sc = sc * sc * h * h / kPi;
+    ga.scale = sc / (4 * kPi);
+    ga.e1 = e1;
+    ga.out = uk;
+    ga.gmax = gmax;
+    ga.Bg = Bg;
+    StageTimer tm(pl, T_GATHER, ks);
+    for (int r = 0; r < nr; r++)
+        CK(launch_grid_to_fixed(grid + (size_t)r * nc * G, (int64_t)nout * (int64_t)G, gmax + r, Bg,
+                                ks, pl->launches));
+    const int64_t ostride = (int64_t)(nout / 2) * g->nt;
+    CK(launch_gather_fix_multi(ga, nout, nr, (int64_t)(nc * G), ostride, ks, pl->launches));
+    for (int r = 0; r < nr; r++) {                   // (the FP64 gather: returns at once unless non-finite)
+        GatherArgs gr = ga;
+        gr.grid = grid + (size_t)r * nc * G;
+        gr.gmax = gmax + r;
+        gr.out = uk + r * ostride;
+        CK(launch_gather_fp64_fallback(gr, nout, ks, pl->launches));
+    }
+    return SE2P_OK;
+}
+
 int se2p_geom_create(se2p_plan pl, const se2p_params *prm, const double *psrc, int64_t ns,
                      const double *ptar, int64_t nt, const double *n, int kinds, se2p_geom *geom)
 {
@@ -1948,7 +2114,57 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
     CKS(ensure_t(pl, S_GCOEFF, (size_t)kBatch * ncf * nsz, &cff));
     if (g->slp) CKS(ensure_t(pl, S_GUR0, (size_t)kBatch * nt, &ur0));
     if (g->dlp) CKS(ensure_t(pl, S_GUR1, (size_t)kBatch * nt, &ur1));
-    for (int r0 = 0; r0 < nrhs; r0 += kBatch) {
+    int mkY = 0, mmult = 1;
+    double mkfac = 1.0;
+    const bool multi = geom_multi_ok(g, &mkY, &mkfac, &mmult);
+    for (int r0 = 0; r0 < nrhs && multi; r0 += kBatch) {
+        // k space of the batch in one pass (geom_kspace_multi) on the plan's
+        // stream, the stored real-space operator beside it on the side stream
+        const int nb = std::min(kBatch, nrhs - r0);
+        for (int r = 0; r < nb; r++) {
+            const double2 *fs = g->slp ? g->fin + (size_t)(r0 + r) * ns : nullptr;
+            const double2 *fd = g->dlp ? g->din + (size_t)(r0 + r) * ns : nullptr;
+            double *cr = coef + (size_t)r * nc * nsz;
+            CK(launch_src_coef(ns, g->sperm, fs, fd, g->nr, cr, nc, st, pl->launches));
+            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf * nsz, ncf,
+                                  st, pl->launches));
+        }
+        CK(cudaEventRecord(pl->fork, st));
+        CK(cudaStreamWaitEvent(pl->side, pl->fork, 0));
+        {
+            StageTimer tm(pl, T_REAL, pl->side);
+            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nnz, g->rowptr, g->src, g->cf, cff, ncf,
+                                 doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+                                 (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, pl->side, pl->launches));
+        }
+        CK(cudaEventRecord(pl->join, pl->side));
+        double2 *uk = nullptr, *zm = nullptr, *part = nullptr;
+        const int nk2 = (g->slp ? 1 : 0) + (g->dlp ? 1 : 0);
+        CKS(ensure_t(pl, S_MUK, (size_t)kBatch * nk2 * nt, &uk));
+        CKS(geom_kspace_multi(g, nb, coef, (int64_t)nc * (int64_t)nsz, st, uk));
+        if (g->dlp) {
+            CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
+            CKS(ensure_t(pl, S_MZM, (size_t)kBatch, &zm));
+            StageTimer tm(pl, T_ZERO_MODE);
+            for (int r = 0; r < nb; r++)             // sum over the caller's (unwrapped) sources
+                CK(launch_zero_mode(ns, g->ps, g->din + (size_t)(r0 + r) * ns, g->nr,
+                                    1.0 / (g->prm.Lx * g->prm.Ly), part, zm + r, st, pl->launches));
+        }
+        CK(cudaStreamWaitEvent(st, pl->join, 0));
+        StageTimer tm(pl, T_ASSEMBLE);
+        for (int r = 0; r < nb; r++) {
+            const int rr = r0 + r;
+            const double2 *ukr = uk + (size_t)r * nk2 * nt;
+            if (g->slp)
+                CK(launch_assemble(nt, 3, g->tperm, ur0 + (size_t)r * nt, ukr, nullptr,
+                                   uo_slp + (size_t)rr * nt, nullptr, nullptr, st, pl->launches));
+            if (g->dlp)
+                CK(launch_assemble(nt, 4, g->tperm, ur1 + (size_t)r * nt, ukr + (g->slp ? nt : 0),
+                                   zm + r, uo_dlp + (size_t)rr * nt, nullptr, nullptr, st,
+                                   pl->launches));
+        }
+    }
+    for (int r0 = 0; r0 < nrhs && !multi; r0 += kBatch) {
         const int nb = std::min(kBatch, nrhs - r0);
         // real space: float-float coefficients of each RHS, then the sparse product
         for (int r = 0; r < nb; r++) {

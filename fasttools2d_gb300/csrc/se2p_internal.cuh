@@ -503,6 +503,17 @@ cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mu
                                 cudaStream_t st, int64_t &launches);
 cudaError_t launch_spread_fix(const SpreadArgs &a, int nc, int kY, cudaStream_t st,
                               int64_t &launches);
+// Many right-hand sides on one point set: k_spread_fix and k_gather_fix
+// with the per-point Gaussian factors formed once for all nr of them
+// (coefficients, grids, bound slots, outputs strided by right-hand side), and
+// the FP64 gather alone (it runs where the grid holds a non-finite value).
+cudaError_t launch_spread_fix_multi(const SpreadArgs &a, int nc, int kY, int nr, int64_t cstride,
+                                    int64_t gstride, int bstride, cudaStream_t st,
+                                    int64_t &launches);
+cudaError_t launch_gather_fix_multi(const GatherArgs &a, int nc, int nr, int64_t gstride,
+                                    int64_t ostride, cudaStream_t st, int64_t &launches);
+cudaError_t launch_gather_fp64_fallback(const GatherArgs &a, int nc, cudaStream_t st,
+                                        int64_t &launches);
 cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
                                     const unsigned long long *bound, double2 *z, cudaStream_t st,
                                     int64_t &launches);

@@ -1578,9 +1578,13 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix(SpreadArgs a, 
     const bool once = a.Mx > a.P && a.My > a.P;      // a stencil wraps at most once
     long long *grid = reinterpret_cast<long long *>(a.grid);
     const int64_t nw = (int64_t)gridDim.x * kSpreadWarps;
-    for (int64_t base = ((int64_t)blockIdx.x * kSpreadWarps + wid) * 32; base < a.ns;
-         base += nw * 32) {
-        const int64_t sl = base + lane;
+    // Batch k of warp w holds the sources k 32 nw + w + lane nw: all warps
+    // walk the box-sorted sources together, nw apart, so the grid band they
+    // update at any time spans about nw sources' stencils and stays in L2
+    // (32 consecutive sources per warp kept a third of the grids live).
+    const int64_t sstep = nw;
+    for (int64_t base = (int64_t)blockIdx.x * kSpreadWarps + wid; base < a.ns; base += nw * 32) {
+        const int64_t sl = base + (int64_t)lane * sstep;
         int mx = 0, my = 0;
         double Ax = 0.0, Ay = 0.0, e3x = 1.0, e3y = 1.0;
         double cf[NC];
@@ -1597,7 +1601,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix(SpreadArgs a, 
 #pragma unroll
             for (int c = 0; c < NC; c++) cf[c] = a.coef[NC * sl + c];
         }
-        const int cnt = (int)min((int64_t)32, a.ns - base);
+        const int cnt = (int)min((int64_t)32, (a.ns - base + sstep - 1) / sstep);   // lanes holding one
         for (int j = 0; j < cnt; j++) {
             const int smx = __shfl_sync(~0u, mx, j), smy = __shfl_sync(~0u, my, j);
             const double sAx = __shfl_sync(~0u, Ax, j), sAy = __shfl_sync(~0u, Ay, j);
@@ -1658,6 +1662,115 @@ template __global__ void k_spread_fix<2>(SpreadArgs, int);
 template __global__ void k_spread_fix<3>(SpreadArgs, int);
 template __global__ void k_spread_fix<4>(SpreadArgs, int);
 template __global__ void k_spread_fix<5>(SpreadArgs, int);
+
+// k_spread_fix for nr right-hand sides on one point set (many densities per
+// geometry): the stencil origin, exponentials and factor scans of a source
+// are formed once, then each right-hand side r spreads its NC coefficients
+// (a.coef + r cstride, NC per source) into its own grids (a.grid + r gstride
+// words) at its own scale (bound slot a.bound[r bstride]).  A right-hand side
+// whose slot is kFixedOff is left to the FP64 spread.  The grids are the same
+// integers k_spread_fix gives for each right-hand side alone.
+template <int NC>
+__global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix_multi(SpreadArgs a, int kY, int nr,
+                                                                        int64_t cstride,
+                                                                        int64_t gstride, int bstride)
+{
+    __shared__ long long xsh[kSpreadWarps][NC][32];
+    __shared__ long long ysh[kSpreadWarps][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P1 = a.P + 1, NN = P1 * P1;            // P1 <= 31
+    const size_t G = (size_t)a.Mx * a.My;
+    const double sy = ldexp(1.0, 62 - kY);
+    const int di = 32 / P1, dj = 32 - di * P1, i0 = lane / P1, j0 = lane - i0 * P1;
+    const bool once = a.Mx > a.P && a.My > a.P;      // a stencil wraps at most once
+    const int64_t nw = (int64_t)gridDim.x * kSpreadWarps;
+    // Batch k of warp w holds the sources k 32 nw + w + lane nw: all warps
+    // walk the box-sorted sources together, nw apart, so the grid band they
+    // update at any time spans about nw sources' stencils and stays in L2
+    // (32 consecutive sources per warp kept a third of the grids live).
+    const int64_t sstep = nw;
+    for (int64_t base = (int64_t)blockIdx.x * kSpreadWarps + wid; base < a.ns; base += nw * 32) {
+        const int64_t sl = base + (int64_t)lane * sstep;
+        int mx = 0, my = 0;
+        double Ax = 0.0, Ay = 0.0, e3x = 1.0, e3y = 1.0;
+        if (sl < a.ns) {
+            const double2 Sp = a.sp[sl];
+            double px, py;
+            closest_node(Sp.x, Sp.y, a.Lhx, a.Lhy, a.h, a.P, mx, my, px, py);
+            Ax = exp(a.a * (px * px + 2.0 * a.w * px));
+            Ay = exp(a.a * (py * py + 2.0 * a.w * py)) * sy;
+            e3x = exp(-2.0 * a.a * a.h * px);
+            e3y = exp(-2.0 * a.a * a.h * py);
+        }
+        const int cnt = (int)min((int64_t)32, (a.ns - base + sstep - 1) / sstep);   // lanes holding one
+        for (int j = 0; j < cnt; j++) {
+            const int smx = __shfl_sync(~0u, mx, j), smy = __shfl_sync(~0u, my, j);
+            const double sAx = __shfl_sync(~0u, Ax, j), sAy = __shfl_sync(~0u, Ay, j);
+            const double b3x = __shfl_sync(~0u, e3x, j), b3y = __shfl_sync(~0u, e3y, j);
+            double px_ = lane >= 1 ? b3x : 1.0;
+            double py_ = lane >= 1 ? b3y : 1.0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double tx = __shfl_up_sync(~0u, px_, o);
+                const double ty = __shfl_up_sync(~0u, py_, o);
+                if (lane >= o) {
+                    px_ *= tx;
+                    py_ *= ty;
+                }
+            }
+            double X = 0.0;
+            if (lane < P1) {
+                const double e1v = a.e1[lane];
+                X = sAx * e1v * px_;
+                ysh[wid][lane] = __double2ll_rn(sAy * e1v * py_);
+            }
+            const int c0 = wrap_index(smx, a.Mx), r0 = wrap_index(smy, a.My);
+            for (int r = 0; r < nr; r++) {
+                const unsigned long long bnd = a.bound[(int64_t)r * bstride];
+                if (bnd == kFixedOff) continue;      // (uniform) this one runs the FP64 spread
+                // the scale is a power of two, so X sx rounds as k_spread_fix's factors do
+                const double Xs = X * ldexp(1.0, fix_shift(bnd) + 3 + kY);
+                __syncwarp();
+                if (lane < P1) {
+                    const double *cf = a.coef + r * cstride + (int64_t)NC * (base + (int64_t)j * sstep);
+#pragma unroll
+                    for (int c = 0; c < NC; c++) xsh[wid][c][lane] = __double2ll_rn(cf[c] * Xs);
+                }
+                __syncwarp();
+                long long *grid = reinterpret_cast<long long *>(a.grid) + r * gstride;
+                int i = i0, jj = j0;
+                for (int qd = lane; qd < NN; qd += 32) {
+                    int col = c0 + i, row = r0 + jj;
+                    if (once) {
+                        col = col >= a.Mx ? col - a.Mx : col;
+                        row = row >= a.My ? row - a.My : row;
+                    } else {
+                        col %= a.Mx;
+                        row %= a.My;
+                    }
+                    const long long y = ysh[wid][jj];
+                    unsigned long long *g =
+                        reinterpret_cast<unsigned long long *>(grid + (size_t)col * a.My + row);
+#pragma unroll
+                    for (int c = 0; c < NC; c++)
+                        atomicAdd(g + c * G,
+                                  (unsigned long long)((__mul64hi(xsh[wid][c][i], y) + 1) >> 1));
+                    i += di;
+                    jj += dj;
+                    if (jj >= P1) {
+                        jj -= P1;
+                        i++;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template __global__ void k_spread_fix_multi<2>(SpreadArgs, int, int, int64_t, int64_t, int);
+template __global__ void k_spread_fix_multi<3>(SpreadArgs, int, int, int64_t, int64_t, int);
+template __global__ void k_spread_fix_multi<5>(SpreadArgs, int, int, int64_t, int64_t, int);
 
 // ===========================================================================
 // 2D real FFT as two 1D complex passes (FP64 form).
@@ -2221,6 +2334,90 @@ template __global__ void k_gather_fix<2, 12>(GatherArgs);
 template __global__ void k_gather_fix<4, 12>(GatherArgs);
 template __global__ void k_gather_fix<2, 0>(GatherArgs);
 template __global__ void k_gather_fix<4, 0>(GatherArgs);
+
+// k_gather_fix for nr right-hand sides on one point set: a target's stencil
+// origin and Gaussian factors are formed once, then each right-hand side r
+// gathers its NC fixed-point grids (a.grid + r gstride words, scale from
+// a.gmax[r]) into a.out + r ostride.  A right-hand side whose grid held a
+// non-finite value is left to the FP64 gather.
+template <int NC, int PT>
+__global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int nr, int64_t gstride,
+                                                             int64_t ostride)
+{
+    const int P = PT > 0 ? PT : a.P;
+    const long long bias = P / 2 + 1;
+    const size_t G = (size_t)a.Mx * a.My;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nt;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const double2 T = a.tp[t];
+        int mx, my;
+        double px, py;
+        closest_node(T.x, T.y, a.Lhx, a.Lhy, a.h, P, mx, my, px, py);
+        const double ax = exp(a.a * (px * px + 2.0 * a.w * px)) * 0x1p62;
+        const double ay = exp(a.a * (py * py + 2.0 * a.w * py)) * 0x1p62;
+        const double e3x = exp(-2.0 * a.a * a.h * px);
+        const double e3y = exp(-2.0 * a.a * a.h * py);
+        long long yq[(PT > 0 ? PT : kMaxP) + 1];
+        {
+            double ey = ay;
+#pragma unroll
+            for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                if (j <= P) {
+                    yq[j] = __double2ll_rn(a.e1[j] * ey);
+                    ey *= e3y;
+                }
+            }
+        }
+        const bool rows_inside = my >= 0 && my + P < a.My;
+        for (int r = 0; r < nr; r++) {
+            const unsigned long long gb = a.gmax[r];
+            if (gb >= kGridNonFinite) continue;      // this one runs the FP64 gather
+            const double outs = gb == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gb, a.Bg));
+            const long long *grid = reinterpret_cast<const long long *>(a.grid) + r * gstride;
+            long long acc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++) acc[c] = bias;
+            double xf = ax;
+            for (int i = 0; i <= P; i++) {
+                const long long *g = grid + (size_t)wrap_index(mx + i, a.Mx) * a.My;
+                long long tc[NC];
+#pragma unroll
+                for (int c = 0; c < NC; c++) tc[c] = bias;
+                if (rows_inside) {
+                    const long long *gr = g + my;
+#pragma unroll
+                    for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                        if (j <= P) {
+#pragma unroll
+                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
+                        if (j <= P) {
+                            const int row = wrap_index(my + j, a.My);
+#pragma unroll
+                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
+                        }
+                    }
+                }
+                const long long xq = __double2ll_rn(xf * a.e1[i]);
+                xf *= e3x;
+#pragma unroll
+                for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
+            }
+            double2 *out = a.out + r * ostride;
+#pragma unroll
+            for (int k = 0; k < NC / 2; k++)
+                out[k * a.nt + t] = make_double2((double)acc[2 * k] * outs, (double)acc[2 * k + 1] * outs);
+        }
+    }
+}
+template __global__ void k_gather_fix_multi<2, 24>(GatherArgs, int, int64_t, int64_t);
+template __global__ void k_gather_fix_multi<4, 24>(GatherArgs, int, int64_t, int64_t);
+template __global__ void k_gather_fix_multi<2, 0>(GatherArgs, int, int64_t, int64_t);
+template __global__ void k_gather_fix_multi<4, 0>(GatherArgs, int, int64_t, int64_t);
 
 
 // ===========================================================================
@@ -3146,6 +3343,60 @@ cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mu
         launches++;
     }
     k_spread_bin_max<<<stream_grid(nb), 256, 0, st>>>(ws, cnt, nbx, nby, kfac, mult, bound);
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spread_fix_multi(const SpreadArgs &a, int nc, int kY, int nr, int64_t cstride,
+                                    int64_t gstride, int bstride, cudaStream_t st,
+                                    int64_t &launches)
+{
+    if (a.ns <= 0 || nr <= 0) return cudaSuccess;
+    const int64_t warps = (a.ns + 31) / 32;
+    const int64_t want = (warps + kSpreadWarps - 1) / kSpreadWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const unsigned g = (unsigned)(want < cap ? want : cap);
+    switch (nc) {
+    case 2: k_spread_fix_multi<2><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    case 3: k_spread_fix_multi<3><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    case 5: k_spread_fix_multi<5><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    default: return cudaErrorInvalidValue;
+    }
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_fix_multi(const GatherArgs &a, int nc, int nr, int64_t gstride,
+                                    int64_t ostride, cudaStream_t st, int64_t &launches)
+{
+    if (a.nt <= 0 || nr <= 0) return cudaSuccess;
+    const unsigned gf = std::min(grid_for(a.nt, 256), (unsigned)sm_count() * 2);
+    if (nc == 2) {
+        if (a.P == 24) k_gather_fix_multi<2, 24><<<gf, 256, 0, st>>>(a, nr, gstride, ostride);
+        else k_gather_fix_multi<2, 0><<<gf, 256, 0, st>>>(a, nr, gstride, ostride);
+    } else {
+        if (a.P == 24) k_gather_fix_multi<4, 24><<<gf, 256, 0, st>>>(a, nr, gstride, ostride);
+        else k_gather_fix_multi<4, 0><<<gf, 256, 0, st>>>(a, nr, gstride, ostride);
+    }
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_fp64_fallback(const GatherArgs &a, int nc, cudaStream_t st,
+                                        int64_t &launches)
+{
+    if (a.nt <= 0) return cudaSuccess;
+    unsigned g = grid_for(a.nt, 256);
+    if (g > (unsigned)sm_count()) g = (unsigned)sm_count();
+    if (nc == 2) {
+        if (a.P == 24) k_gather<2, 24><<<g, 256, 0, st>>>(a);
+        else if (a.P == 12) k_gather<2, 12><<<g, 256, 0, st>>>(a);
+        else k_gather<2, 0><<<g, 256, 0, st>>>(a);
+    } else {
+        if (a.P == 24) k_gather<4, 24><<<g, 256, 0, st>>>(a);
+        else if (a.P == 12) k_gather<4, 12><<<g, 256, 0, st>>>(a);
+        else k_gather<4, 0><<<g, 256, 0, st>>>(a);
+    }
     launches++;
     return cudaGetLastError();
 }

@@ -55,6 +55,34 @@ def test_geometry_matches_single_rhs(ft, nrhs):
     plan.close()
 
 
+def test_geometry_batched_kspace_per_rhs_fallbacks(ft):
+    """The batched k space of one apply (one spread and one gather launch for
+    all right-hand sides) takes the FP64 spread and gather for a right-hand
+    side with a non-finite density, without touching the others: that one's
+    results are non-finite where a single evaluation's are, the others match
+    single evaluations."""
+    p, q, n, f, g = _cloud(6000, 77, 3)
+    f[1, 0, 123] = np.nan
+    prm = ft.EwaldParams.derived(60.0, 12, 12, 96, 96, 24, 1.0, 1.0)
+    plan = ft.Plan(0)
+    geo = ft.Geometry(p, q, prm, n=n, plan=plan)
+    us, ud = geo.apply(f, g)
+    for r in range(3):
+        vs, vd = ft.stokes_ewald(p, q, f[r], g[r], n, prm, plan=plan)
+        assert np.array_equal(np.isfinite(us[r]), np.isfinite(vs))
+        if r != 1:
+            assert np.isfinite(us[r]).all()
+            assert relerr(us[r], vs) < SINGLE, relerr(us[r], vs)
+            assert relerr(ud[r], vd) < SINGLE, relerr(ud[r], vd)
+        else:
+            # both runs took the FP64 spread, whose atomics add in varying
+            # order; the stresslet's k space amplifies that rounding
+            assert relerr(ud[r], vd) < 1e-11, relerr(ud[r], vd)
+    assert not np.isfinite(us[1]).all()
+    geo.close()
+    plan.close()
+
+
 @pytest.mark.parametrize("kind", ["slp", "dlp"])
 def test_geometry_single_kind(ft, kind):
     p, q, n, f, g = _cloud(8000, 7, 2)
