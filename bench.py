@@ -84,9 +84,9 @@ UNIT = "evals/s"
 C_IN, C_OUT = 5, 4
 SPREAD_RED_PER_SOURCE = (P + 1) ** 2 * C_IN
 FILTER_FLOP_PER_MODE = 60
-DRAM_BYTES = {"spread": 2.008e9, "gather": 0.279e9, "real": 0.182e9}
-REAL_WARP_INST_PER_PAIR = 42.7     # ncu smsp__inst_executed / SLP+DLP pair evaluations
-REAL_FP32_INST_PER_EVAL = 542.0    # ncu FADD 360 + FFMA 125 + FMUL 57 thread instructions per evaluation
+DRAM_BYTES = {"spread": 1.800e9, "gather": 0.277e9, "real": 0.213e9}
+REAL_WARP_INST_PER_PAIR = 41.3     # ncu smsp__inst_executed / SLP+DLP pair evaluations
+REAL_FP32_INST_PER_EVAL = 608.0    # ncu FADD 425 + FFMA 130 + FMUL 52 thread instructions per evaluation
 GATHER_WARP_INST_PER_TARGET = 1508.0   # ncu smsp__inst_executed / targets (k_gather_fix<4,24>)
 # Algorithmic HBM bytes of one launch, each array read or written once:
 # real space reads per sorted source its position (16 B), FP32 copy (8 B), 5
@@ -329,8 +329,8 @@ XI4, RC4, M4, P4 = 860.0, 0.0042, 2048, 12
 
 
 # ncu dram__bytes_read + _write of one launch of the FP32-grid k-space kernels
-# at the mixed-precision workload (profiles/), None until captured.
-F32_DRAM_BYTES = {"spread": None, "gather": None}
+# at the mixed-precision workload (profiles/).
+F32_DRAM_BYTES = {"spread": 0.172e9, "gather": 0.0955e9}
 
 
 def mixed_precision_leg(plan, tens, u_dev, N, steps, timed, dev, with_oracle):
