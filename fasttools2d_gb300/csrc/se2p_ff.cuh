@@ -90,6 +90,50 @@ __device__ __forceinline__ float2 ff_mul(float2 a, float2 b)
     return make_float2(h, l);
 }
 
+// a1 b1 + a2 b2 (+ a3 b3): the products' exact heads summed by TwoSum, their
+// FMA-formed errors and the TwoSum errors added in the tail, normalised once.
+__device__ __forceinline__ float2 ff_dot2(float2 a1, float2 b1, float2 a2, float2 b2)
+{
+    const float p1 = a1.x * b1.x;
+    float e1 = fmaf(a1.x, b1.x, -p1);
+    e1 = fmaf(a1.x, b1.y, e1);
+    e1 = fmaf(a1.y, b1.x, e1);
+    const float p2 = a2.x * b2.x;
+    float e2 = fmaf(a2.x, b2.x, -p2);
+    e2 = fmaf(a2.x, b2.y, e2);
+    e2 = fmaf(a2.y, b2.x, e2);
+    float s, t;
+    two_sum(p1, p2, s, t);
+    t += e1 + e2;
+    float h, l;
+    fast_two_sum(s, t, h, l);
+    return make_float2(h, l);
+}
+
+__device__ __forceinline__ float2 ff_dot3(float2 a1, float2 b1, float2 a2, float2 b2, float2 a3,
+                                          float2 b3)
+{
+    const float p1 = a1.x * b1.x;
+    float e1 = fmaf(a1.x, b1.x, -p1);
+    e1 = fmaf(a1.x, b1.y, e1);
+    e1 = fmaf(a1.y, b1.x, e1);
+    const float p2 = a2.x * b2.x;
+    float e2 = fmaf(a2.x, b2.x, -p2);
+    e2 = fmaf(a2.x, b2.y, e2);
+    e2 = fmaf(a2.y, b2.x, e2);
+    const float p3 = a3.x * b3.x;
+    float e3 = fmaf(a3.x, b3.x, -p3);
+    e3 = fmaf(a3.x, b3.y, e3);
+    e3 = fmaf(a3.y, b3.x, e3);
+    float s, t, u, v;
+    two_sum(p1, p2, s, t);
+    two_sum(s, p3, u, v);
+    t += v + (e1 + e2 + e3);
+    float h, l;
+    fast_two_sum(u, t, h, l);
+    return make_float2(h, l);
+}
+
 // Dot-product accumulator: (s, c) += a * b with a, b float-float.  The
 // product's exact head and the TwoSum error go to the float c; s stays the
 // running float sum (Ogita-Rump-Oishi Dot2 with float-float operands).

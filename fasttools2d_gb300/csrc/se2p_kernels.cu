@@ -535,21 +535,33 @@ __device__ __forceinline__ void real_pair_ff(const RealArgs &a, const RealWarp &
     if (SLP && (fl & 1)) {
         const float2 f1 = cf[0], f2 = cf[1];
         const float2 h = ff_scale(ff_mul(ex, ff_g_e1(x, a.gtab)), 0.5f);
-        const float2 gq = ff_mul(ff_mul(ex, ir2), ff_sub(ff_mul(x1, f2), ff_mul(x2, f1)));
-        s1 = ff_add(s1, ff_add(ff_mul(h, f1), ff_mul(gq, x2)));
-        s2 = ff_add(s2, ff_sub(ff_mul(h, f2), ff_mul(gq, x1)));
+        const float2 gq = ff_mul(ff_mul(ex, ir2), ff_dot2(x1, f2, ff_neg(x2), f1));
+        // the lane's sums as Dot2 accumulators (running float sum, float
+        // compensation): each product's exact head and error go straight in,
+        // and the pair renormalises the sum once (a lane may sum hundreds of
+        // pairs of one target where the boxes are large)
+        ff_dot_acc(h, f1, s1.x, s1.y);
+        ff_dot_acc(gq, x2, s1.x, s1.y);
+        ff_dot_acc(h, f2, s2.x, s2.y);
+        ff_dot_acc(ff_neg(gq), x1, s2.x, s2.y);
+        s1 = ff_norm(s1.x, s1.y);
+        s2 = ff_norm(s2.x, s2.y);
     }
     if (DLP && (fl & 2)) {
         const float2 *Sc = cf + a.doff_ff;
         const float2 S11 = Sc[0], S1221 = Sc[1], S22 = Sc[2], T1 = Sc[3], T2 = Sc[4];
         const float2 fb = ff_scale(ff_mul(ff_add_f(x, 1.0f), ff_sqr(ir2)), -4.0f);
-        const float2 Q = ff_add(ff_add(ff_mul(ff_sqr(x1), S11), ff_mul(ff_mul(x1, x2), S1221)),
-                                ff_mul(ff_sqr(x2), S22));
-        const float2 A1 = ff_add(ff_mul(x1, T1), ff_mul(x2, S1221));
-        const float2 A2 = ff_add(ff_mul(x2, T2), ff_mul(x1, S1221));
+        const float2 Q = ff_dot3(ff_sqr(x1), S11, ff_mul(x1, x2), S1221, ff_sqr(x2), S22);
+        const float2 A1 = ff_dot2(x1, T1, x2, S1221);
+        const float2 A2 = ff_dot2(x2, T2, x1, S1221);
         const float2 fq = ff_mul(fb, Q);
-        d1 = ff_add(d1, ff_mul(ex, ff_add(ff_mul(fq, x1), ff_mul(pf, A1))));
-        d2 = ff_add(d2, ff_mul(ex, ff_add(ff_mul(fq, x2), ff_mul(pf, A2))));
+        const float2 efq = ff_mul(ex, fq), epf = ff_mul(ex, pf);
+        ff_dot_acc(efq, x1, d1.x, d1.y);
+        ff_dot_acc(epf, A1, d1.x, d1.y);
+        ff_dot_acc(efq, x2, d2.x, d2.y);
+        ff_dot_acc(epf, A2, d2.x, d2.y);
+        d1 = ff_norm(d1.x, d1.y);
+        d2 = ff_norm(d2.x, d2.y);
     }
 }
 
