@@ -1502,6 +1502,16 @@ template __global__ void k_spread<5>(SpreadArgs);
 // ===========================================================================
 constexpr int kFixedMaxCover = 1 << 14;
 
+// High 64 bits of the 128-bit product a b, for signed a and 0 <= b < 2^63
+// (b a Gaussian factor): the unsigned high product of a's bit pattern, less b
+// where a is negative (two's complement).  Equal to __mul64hi(a, b), without
+// the correction for a negative b.
+__device__ __forceinline__ long long mulhi_s_u(long long a, long long b)
+{
+    const long long h = (long long)__umul64hi((unsigned long long)a, (unsigned long long)b);
+    return a < 0 ? h - b : h;
+}
+
 
 int spread_bins(int M, int P)
 {
@@ -1574,7 +1584,7 @@ __global__ void k_spread_bin_max(const double *__restrict__ bins, const int *__r
 }
 
 template <int NC>
-__global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix(SpreadArgs a, int kY)
+__global__ void __launch_bounds__(kSpreadWarps * 32, 4) k_spread_fix(SpreadArgs a, int kY)
 {
     __shared__ long long xsh[kSpreadWarps][NC][32];
     __shared__ long long ysh[kSpreadWarps][32];
@@ -1657,7 +1667,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix(SpreadArgs a, 
 #pragma unroll
                 for (int c = 0; c < NC; c++)
                     atomicAdd(g + c * G,
-                              (unsigned long long)((__mul64hi(xsh[wid][c][i], y) + 1) >> 1));
+                              (unsigned long long)((mulhi_s_u(xsh[wid][c][i], y) + 1) >> 1));
                 i += di;
                 jj += dj;
                 if (jj >= P1) {
@@ -1683,7 +1693,7 @@ template __global__ void k_spread_fix<5>(SpreadArgs, int);
 // whose slot is kFixedOff is left to the FP64 spread.  The grids are the same
 // integers k_spread_fix gives for each right-hand side alone.
 template <int NC>
-__global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix_multi(SpreadArgs a, int kY, int nr,
+__global__ void __launch_bounds__(kSpreadWarps * 32, 4) k_spread_fix_multi(SpreadArgs a, int kY, int nr,
                                                                         int64_t cstride,
                                                                         int64_t gstride, int bstride)
 {
@@ -1766,7 +1776,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_fix_multi(SpreadAr
 #pragma unroll
                     for (int c = 0; c < NC; c++)
                         atomicAdd(g + c * G,
-                                  (unsigned long long)((__mul64hi(xsh[wid][c][i], y) + 1) >> 1));
+                                  (unsigned long long)((mulhi_s_u(xsh[wid][c][i], y) + 1) >> 1));
                     i += di;
                     jj += dj;
                     if (jj >= P1) {
@@ -2317,7 +2327,7 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
                 for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
                     if (j <= P) {
 #pragma unroll
-                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
+                        for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(gr + c * G + j), yq[j]);
                     }
                 }
             } else {
@@ -2326,14 +2336,14 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
                     if (j <= P) {
                         const int row = wrap_index(my + j, a.My);
 #pragma unroll
-                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
+                        for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(g + c * G + row), yq[j]);
                     }
                 }
             }
             const long long xq = __double2ll_rn(xf * a.e1[i]);
             xf *= e3x;
 #pragma unroll
-            for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
+            for (int c = 0; c < NC; c++) acc[c] += mulhi_s_u(tc[c], xq);
         }
 #pragma unroll
         for (int k = 0; k < NC / 2; k++)
@@ -2401,7 +2411,7 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
                     for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
                         if (j <= P) {
 #pragma unroll
-                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
+                            for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(gr + c * G + j), yq[j]);
                         }
                     }
                 } else {
@@ -2410,14 +2420,14 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
                         if (j <= P) {
                             const int row = wrap_index(my + j, a.My);
 #pragma unroll
-                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
+                            for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(g + c * G + row), yq[j]);
                         }
                     }
                 }
                 const long long xq = __double2ll_rn(xf * a.e1[i]);
                 xf *= e3x;
 #pragma unroll
-                for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
+                for (int c = 0; c < NC; c++) acc[c] += mulhi_s_u(tc[c], xq);
             }
             double2 *out = a.out + r * ostride;
 #pragma unroll
