@@ -1505,7 +1505,8 @@ constexpr int kFixedMaxCover = 1 << 14;
 // High 64 bits of the 128-bit product a b, for signed a and 0 <= b < 2^63
 // (b a Gaussian factor): the unsigned high product of a's bit pattern, less b
 // where a is negative (two's complement).  Equal to __mul64hi(a, b), without
-// the correction for a negative b.
+// the correction for a negative b.  (The integer spread gains 0.2 ms from it;
+// the integer gather runs slightly faster with __mul64hi and keeps it.)
 __device__ __forceinline__ long long mulhi_s_u(long long a, long long b)
 {
     const long long h = (long long)__umul64hi((unsigned long long)a, (unsigned long long)b);
@@ -2327,7 +2328,7 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
                 for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
                     if (j <= P) {
 #pragma unroll
-                        for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(gr + c * G + j), yq[j]);
+                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
                     }
                 }
             } else {
@@ -2336,14 +2337,14 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
                     if (j <= P) {
                         const int row = wrap_index(my + j, a.My);
 #pragma unroll
-                        for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(g + c * G + row), yq[j]);
+                        for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
                     }
                 }
             }
             const long long xq = __double2ll_rn(xf * a.e1[i]);
             xf *= e3x;
 #pragma unroll
-            for (int c = 0; c < NC; c++) acc[c] += mulhi_s_u(tc[c], xq);
+            for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
         }
 #pragma unroll
         for (int k = 0; k < NC / 2; k++)
@@ -2411,7 +2412,7 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
                     for (int j = 0; j <= (PT > 0 ? PT : kMaxP); j++) {
                         if (j <= P) {
 #pragma unroll
-                            for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(gr + c * G + j), yq[j]);
+                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(gr + c * G + j), yq[j]);
                         }
                     }
                 } else {
@@ -2420,14 +2421,14 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
                         if (j <= P) {
                             const int row = wrap_index(my + j, a.My);
 #pragma unroll
-                            for (int c = 0; c < NC; c++) tc[c] += mulhi_s_u(__ldg(g + c * G + row), yq[j]);
+                            for (int c = 0; c < NC; c++) tc[c] += __mul64hi(__ldg(g + c * G + row), yq[j]);
                         }
                     }
                 }
                 const long long xq = __double2ll_rn(xf * a.e1[i]);
                 xf *= e3x;
 #pragma unroll
-                for (int c = 0; c < NC; c++) acc[c] += mulhi_s_u(tc[c], xq);
+                for (int c = 0; c < NC; c++) acc[c] += __mul64hi(tc[c], xq);
             }
             double2 *out = a.out + r * ostride;
 #pragma unroll
