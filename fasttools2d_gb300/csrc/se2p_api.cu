@@ -157,6 +157,10 @@ struct DeviceGuard {
     int prev = -1;
     explicit DeviceGuard(int dev)
     {
+        // an error left pending by earlier calls of other code is not this
+        // call's: the launch checks below read cudaGetLastError (a sticky
+        // error persists and is still reported)
+        (void)cudaGetLastError();
         if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
         if (prev != dev) cudaSetDevice(dev);
     }
@@ -588,10 +592,10 @@ static int spread(se2p_plan pl, SpreadArgs &sa, int nc, bool allow_fixed, cudaSt
     *fixb = nullptr;
     sa.bound = nullptr;
     if (allow_fixed && spread_fixed_ok(sa, kY, kfac, mult)) {
-        const int64_t nb = (int64_t)spread_bins(sa.Mx, sa.P) * spread_bins(sa.My, sa.P);
         double *ws = nullptr;
-        CKS(ensure_t(pl, S_SBINS, 2 * (size_t)nb + 1, &ws));
-        sa.bound = reinterpret_cast<const unsigned long long *>(ws + nb);
+        CKS(ensure_t(pl, S_SBINS, (size_t)spread_bound_words(sa.Mx, sa.My, sa.P), &ws));
+        sa.bound = reinterpret_cast<const unsigned long long *>(
+            ws + spread_bound_slot(sa.Mx, sa.My, sa.P));
         CK(launch_spread_bound(sa, nc, kfac, mult, ws, ks, pl->launches));
         CK(launch_spread_fix(sa, nc, kY, ks, pl->launches));
         *fixb = sa.bound;
@@ -1047,8 +1051,8 @@ int run(se2p_plan pl, const Job &J, const Io &io)
             double kfac = 1.0;
             if (pl->precision == SE2P_PRECISION_FP64 && spread_fixed_ok(sa, kY, kfac, mult) &&
                 kY == 0) {
-                CKS(ensure_t(pl, S_GMAX, 1, &gmax));
-                CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long), ks));
+                CKS(ensure_t(pl, S_GMAX, kGmaxWords, &gmax));
+                CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long) * kGmaxWords, ks));
                 Bg = gather_fixed_bits(sa);
             }
         }
@@ -1077,7 +1081,7 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ga.gmax = gmax;
         ga.Bg = Bg;
         StageTimer tm(pl, T_GATHER, ks);
-        if (gmax) CK(launch_grid_to_fixed(grid, (int64_t)nout * (int64_t)G, gmax, Bg, ks, pl->launches));
+        if (gmax) CK(launch_grid_to_fixed(grid, nout, (int64_t)G, gmax, Bg, ks, pl->launches));
         CK(launch_gather(ga, nout, ks, pl->launches));
     }
 
@@ -1329,8 +1333,8 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
     const double a_gauss = -2 * J.xi * J.xi / J.eta;
     const bool ffg = form == kFormFF && adj_gather_ff_ok(a_gauss, h, J.w, P);
     if (ffg) {
-        CKS(ensure_t(pl, S_GMAX, 1, &gmax));
-        CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long), ks));
+        CKS(ensure_t(pl, S_GMAX, kGmaxWords, &gmax));
+        CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long) * kGmaxWords, ks));
     }
     {
         StageTimer tm(pl, T_FFT_INV, ks);
@@ -1937,9 +1941,9 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
     CKS(ensure_t(pl, S_SPEC, (size_t)Mx * (My / 2 + 1) * nc, &spec));
     CKS(ensure_t(pl, S_ZGRID, G * (size_t)((nc + 1) / 2), &zg));
     CKS(ensure_t(pl, S_E1, (size_t)P + 1, &e1));
-    CKS(ensure_t(pl, S_MGMAX, (size_t)nr, &gmax));
-    const int64_t nbin = (int64_t)spread_bins(Mx, P) * spread_bins(My, P);
-    const int64_t bstride = 2 * nbin + 1;
+    CKS(ensure_t(pl, S_MGMAX, (size_t)nr * kGmaxWords, &gmax));
+    const int64_t bslot = spread_bound_slot(Mx, My, P);   // the bound slot in each set
+    const int64_t bstride = spread_bound_words(Mx, My, P);
     CKS(ensure_t(pl, S_SBINS, (size_t)bstride * nr, &ws));
     // e1[j] = exp(-2 xi^2/eta h^2 j^2) (mex_stokes_slp_kspace.cpp:64-67)
     double e1h[kMaxP + 1];
@@ -1947,7 +1951,7 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
     for (int j = -P / 2; j <= P / 2; j++) e1h[j + P / 2] = std::exp(t * j * j);
     CK(cudaMemcpyAsync(e1, e1h, sizeof(double) * (P + 1), cudaMemcpyHostToDevice, ks));
     CK(cudaMemsetAsync(grid, 0, sizeof(double) * G * nc * nr, ks));
-    CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long) * nr, ks));
+    CK(cudaMemsetAsync(gmax, 0, sizeof(unsigned long long) * kGmaxWords * nr, ks));
 
     SpreadArgs sa;
     sa.sp = g->sp;
@@ -1967,14 +1971,14 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
         SpreadArgs sr = sa;
         sr.coef = coef + r * cstride;
         sr.grid = grid + (size_t)r * nc * G;
-        sr.bound = reinterpret_cast<const unsigned long long *>(ws + r * bstride + nbin);
+        sr.bound = reinterpret_cast<const unsigned long long *>(ws + r * bstride + bslot);
         return sr;
     };
     {
         StageTimer tm(pl, T_SPREAD, ks);
         for (int r = 0; r < nr; r++)
             CK(launch_spread_bound(rhs_spread(r), nc, kfac, mult, ws + r * bstride, ks, pl->launches));
-        sa.bound = reinterpret_cast<const unsigned long long *>(ws + nbin);
+        sa.bound = reinterpret_cast<const unsigned long long *>(ws + bslot);
         CK(launch_spread_fix_multi(sa, nc, kY, nr, cstride, (int64_t)(nc * G), (int)bstride, ks,
                                    pl->launches));
         for (int r = 0; r < nr; r++)                 // (the FP64 spread: returns at once unless crowded)
@@ -1997,7 +2001,7 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
     fa.transposed = 1;
     for (int r = 0; r < nr; r++) {
         double *gr = grid + (size_t)r * nc * G;
-        const auto *fixb = reinterpret_cast<const unsigned long long *>(ws + r * bstride + nbin);
+        const auto *fixb = reinterpret_cast<const unsigned long long *>(ws + r * bstride + bslot);
         {
             StageTimer tm(pl, T_FFT_FWD, ks);
             CKS(fft_fwd_1d(pl, ks, Mx, My, gr, nc, zg, spec, fixb, true));
@@ -2009,7 +2013,7 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
         }
         {
             StageTimer tm(pl, T_FFT_INV, ks);
-            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, gr, true, gmax + r));
+            CKS(fft_inv_1d(pl, ks, Mx, My, spec, nout, zg, gr, true, gmax + r * kGmaxWords));
         }
     }
     GatherArgs ga;
@@ -2033,14 +2037,14 @@ static int geom_kspace_multi(se2p_geom g, int nr, const double *coef, int64_t cs
     ga.Bg = Bg;
     StageTimer tm(pl, T_GATHER, ks);
     for (int r = 0; r < nr; r++)
-        CK(launch_grid_to_fixed(grid + (size_t)r * nc * G, (int64_t)nout * (int64_t)G, gmax + r, Bg,
-                                ks, pl->launches));
+        CK(launch_grid_to_fixed(grid + (size_t)r * nc * G, nout, (int64_t)G, gmax + r * kGmaxWords,
+                                Bg, ks, pl->launches));
     const int64_t ostride = (int64_t)(nout / 2) * g->nt;
     CK(launch_gather_fix_multi(ga, nout, nr, (int64_t)(nc * G), ostride, ks, pl->launches));
     for (int r = 0; r < nr; r++) {                   // (the FP64 gather: returns at once unless non-finite)
         GatherArgs gr = ga;
         gr.grid = grid + (size_t)r * nc * G;
-        gr.gmax = gmax + r;
+        gr.gmax = gmax + r * kGmaxWords;
         gr.out = uk + r * ostride;
         CK(launch_gather_fp64_fallback(gr, nout, ks, pl->launches));
     }

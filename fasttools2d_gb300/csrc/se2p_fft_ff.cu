@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
             }
             if (p.gmax) {
                 for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(~0u, m, o));
-                if ((threadIdx.x & 31) == 0 && m) atomicMax(p.gmax, m);
+                if ((threadIdx.x & 31) == 0 && m) atomicMax(p.gmax + q, m);
             }
         } else {
             for (int k = threadIdx.x; k < L; k += blockDim.x) {

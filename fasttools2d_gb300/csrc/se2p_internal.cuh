@@ -335,9 +335,10 @@ struct GatherArgs {
     double Lhx, Lhy, h, w, a, scale;
     const double *e1;
     double2 *out;         // NC/2 outputs per target, [k * nt + t]
-    // Fixed-point form (k_gather_fix): *gmax holds the bit pattern of
-    // max |grid| (from the unpack), and launch_grid_to_fixed has turned the
-    // grids into int64 at the scale that gmax and Bg give.
+    // Fixed-point form (k_gather_fix): gmax[q] holds the bit pattern of
+    // max |grid| over grids 2q and 2q+1 (from the unpack; kGmaxWords words),
+    // and launch_grid_to_fixed has turned each grid into int64 at the scale
+    // that its pair's gmax and Bg give.
     const unsigned long long *gmax = nullptr;
     int Bg = 0;
 };
@@ -392,14 +393,16 @@ cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
 // Hermitian join, and the final real/imaginary unpack.
 cudaError_t launch_pack_real_pairs(const double *grid, int nc, int64_t G, double2 *z,
                                    cudaStream_t st, int64_t &launches);
+// With gmax (kGmaxWords words, zeroed), also the largest |value| of each
+// pair of grids, gmax[q] for grids 2q and 2q+1.
 cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, double *grid,
                                      cudaStream_t st, int64_t &launches,
                                      unsigned long long *gmax = nullptr);
-// In place: the n doubles of grid become int64 round(g 2^Sg), max|g| 2^Sg < 2^Bg,
-// unless *gmax marks a non-finite value (then the grid stays as it is and
-// launch_gather runs the FP64 gather).
-cudaError_t launch_grid_to_fixed(double *grid, int64_t n, const unsigned long long *gmax, int Bg,
-                                 cudaStream_t st, int64_t &launches);
+// In place: each of the nout grids of G doubles becomes int64 round(g 2^Sg),
+// max|g| 2^Sg < 2^Bg over its pair (gmax[c / 2]), unless a gmax word marks a
+// non-finite value (then the grids stay as they are and the FP64 gather runs).
+cudaError_t launch_grid_to_fixed(double *grid, int nout, int64_t G, const unsigned long long *gmax,
+                                 int Bg, cudaStream_t st, int64_t &launches);
 cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
                                         cudaStream_t st, int64_t &launches);
 cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,
@@ -427,7 +430,7 @@ struct FftRowsFF {
     int npl_in = 0;
     double *unpack_out = nullptr;     // double planes
     int npl_out = 0;
-    unsigned long long *gmax = nullptr;   // largest |value| unpacked (bit pattern), optional
+    unsigned long long *gmax = nullptr;   // largest |value| unpacked per pair q (bit pattern), optional
 };
 bool fft_rows_ff_plan(int L, FftRowsFF &p);
 void fft_rows_ff_twiddles(int L, float4 *host);   // exp(-2 pi i m/L), m < L, float-float
@@ -481,6 +484,14 @@ cudaError_t launch_spread(const SpreadArgs &a, int nc, cudaStream_t st, int64_t 
 // the grids hold doubles.
 constexpr unsigned long long kFixedOff = ~0ull;      // above every finite bound
 
+// The gather's grid maxima: one bit pattern per pair of output grids (SLP,
+// DLP, and the adjoint's fifth grid), each grid scaled by its own pair's.
+constexpr int kGmaxWords = 3;
+__device__ __forceinline__ unsigned long long gmax_all(const unsigned long long *g)
+{
+    return max(g[0], max(g[1], g[2]));
+}
+
 // Scale S of the fixed-point spread's grids (int64 at 2^S, bound 2^S < 2^59),
 // from the bit pattern of the positive bound.
 __device__ __forceinline__ int fix_shift(unsigned long long bits)
@@ -492,13 +503,16 @@ __device__ __forceinline__ int fix_shift(unsigned long long bits)
     return S < -960 ? -960 : (S > 960 ? 960 : S);
 }
 
-// ws: 2 nb + 1 doubles, nb = spread_bins(Mx, P) * spread_bins(My, P): the
-// per-bin sums of max_c |c|, the bound slot at ws + nb, then nb int counts.
+// ws: spread_bound_words(Mx, My, P) doubles (the bins' sums of max_c |c|,
+// their window along x, the bound slot at spread_bound_slot(Mx, My, P), then
+// the bins' source counts and their window as ints).
 // mult is the number of times one stencil can cover a node (> 1 when M <= P)
 // and kfac = mult 2^(2 kY).  When the bound slot ends up all ones the FP64
 // spread runs (launch it behind launch_spread_fix with a.bound set) and the
 // grids hold doubles.
 int spread_bins(int M, int P);
+int64_t spread_bound_words(int Mx, int My, int P);
+int64_t spread_bound_slot(int Mx, int My, int P);
 cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mult, double *ws,
                                 cudaStream_t st, int64_t &launches);
 cudaError_t launch_spread_fix(const SpreadArgs &a, int nc, int kY, cudaStream_t st,

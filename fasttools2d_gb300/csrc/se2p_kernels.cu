@@ -11,6 +11,8 @@
 // next to the FP64 pipe.
 #include "se2p_internal.cuh"
 
+#include <algorithm>
+
 namespace se2p {
 
 // ===========================================================================
@@ -1483,21 +1485,31 @@ template __global__ void k_spread<5>(SpreadArgs);
 // (the grid is bitwise reproducible), and each contribution is off by at most
 // 3/4 unit of 2^-S, with no bias.
 //
-// The bound (k_spread_bin_sum, k_spread_bin_max): bins of at least P+2 nodes
-// per side hold the sums over their sources of max_c |c|.  A stencil reaches
-// P/2 nodes from its centre node, so a node receives only from sources of its
-// own bin and the 8 adjacent ones, and the largest 3 x 3 bin sum, times the
-// number of times one stencil covers a node when M <= P and times 2^(2 kY),
-// bounds every node's sum.
+// The bound (k_spread_bin_sum, k_bound_x, k_bound_y_max): bins of kBoundBin
+// x kBoundBin nodes hold the sums over their sources of max_c |c|.  A source
+// at node coordinate t gives a node at distance d (in nodes) the factor
+// X Y = exp(a h^2 dx^2) exp(a h^2 dy^2) (times at most 2^(2 kY) when w differs
+// from h P/2), and reaches only |d| <= P/2 + 1.  Between a source's bin and a
+// node's bin k bins apart the distance is at least (k - 1) kBoundBin (one bin
+// less when kBoundBin does not divide M, where the last bin is short), so the
+// bin sums weighted by those largest factors, a separable window of 2R + 1
+// bins per axis, bound every node's sum; its largest value, times 2^(2 kY)
+// and the number of times one stencil covers a node when M <= P, is the
+// bound.  (Bins of P+2 nodes with every factor taken as 1 bounded the sums
+// about 50 times too high; the unit 2^-S scales with the bound, and its
+// rounding noise, white on the grid, is amplified by the deconvolution of the
+// Gaussian in the filter: at eta = 3.3 it reached 3e-13 of the k-space
+// velocity.)  Where the window would wrap onto itself (grids under 2R + 1
+// bins) every bin counts with factor 1.
 //
 // The unit 2^-S is fixed by that bound, i.e. by sum |c|, while FP64 atomics
 // round relative to the partial sums, which grow like sqrt(n) when the signs
 // of the coefficients vary.  Each node's error is about n 2^-59 of its value
 // here against sqrt(n) 2^-53 there, n the number of stencils covering it: the
 // integer sums are the more accurate below n ~ 2^11 and lose beyond.  So when
-// some 3 x 3 bin neighbourhood holds more than kFixedMaxCover stencil covers,
-// k_spread_bin_max marks the bound slot kFixedOff, k_spread_fix returns at
-// once and the FP64 spread (launched behind it) runs instead; the pack reads
+// some window holds more than kFixedMaxCover sources (stencil covers),
+// k_bound_y_max marks the bound slot kFixedOff, the integer spreads return at
+// once and the FP64 spread (launched behind them) runs instead; the pack reads
 // the same mark.  The choice costs no host synchronisation.
 // ===========================================================================
 constexpr int kFixedMaxCover = 1 << 14;
@@ -1514,10 +1526,49 @@ __device__ __forceinline__ long long mulhi_s_u(long long a, long long b)
 }
 
 
+constexpr int kBoundBin = 4;      // nodes per bound bin and axis
+constexpr int kBoundMaxR = 15;
+
 int spread_bins(int M, int P)
 {
-    const int b = M / (P + 2);
-    return b > 1 ? b : 1;
+    (void)P;
+    return (M + kBoundBin - 1) / kBoundBin;
+}
+
+int64_t spread_bound_words(int Mx, int My, int P)
+{
+    return 3 * (int64_t)spread_bins(Mx, P) * spread_bins(My, P) + 1;
+}
+
+int64_t spread_bound_slot(int Mx, int My, int P)
+{
+    return 2 * (int64_t)spread_bins(Mx, P) * spread_bins(My, P);
+}
+
+// One axis of the bound's window: bins within R of a node's bin, and the
+// largest Gaussian factor a source k bins away can give it (full: every bin,
+// factor 1).
+struct BoundAxis {
+    int nb, R, full;
+    double w[kBoundMaxR + 1];
+};
+
+static BoundAxis bound_axis(int M, int P, double a, double h)
+{
+    BoundAxis ax{};
+    ax.nb = spread_bins(M, P);
+    const int slack = M % kBoundBin ? 1 : 0;
+    const int R = (P / 2 + 1) / kBoundBin + 1 + slack;
+    if (2 * R + 1 > ax.nb || R > kBoundMaxR) {
+        ax.full = 1;
+        return ax;
+    }
+    ax.R = R;
+    for (int k = 0; k <= R; k++) {
+        const double d = (double)std::max(0, (k - 1 - slack) * kBoundBin);
+        ax.w[k] = std::exp(a * h * h * d * d) * (1.0 + 1e-12);
+    }
+    return ax;
 }
 
 // (A NaN or infinite coefficient marks the bound kFixedOff: the FP64 spread
@@ -1538,39 +1589,75 @@ __global__ void k_spread_bin_sum(SpreadArgs a, int nc, int nbx, int nby, double 
         if (!finite) atomicMax(bound, kFixedOff);
         if (!(m > 0.0)) continue;
         const double2 S = a.sp[s];
-        // the stencil's centre node, to within one node
+        // the node cell holding the source, t in [cx, cx + 1) (mod M)
         const int cx = wrap_index((int)floor((S.x + a.Lhx) * inv_h), a.Mx);
         const int cy = wrap_index((int)floor((S.y + a.Lhy) * inv_h), a.My);
-        const int bx = (int)((int64_t)cx * nbx / a.Mx), by = (int)((int64_t)cy * nby / a.My);
+        const int bx = cx / kBoundBin, by = cy / kBoundBin;
         atomicAdd(&bins[(int64_t)bx * nby + by], m);
         atomicAdd(&cnt[(int64_t)bx * nby + by], 1);
     }
 }
 
-__global__ void k_spread_bin_max(const double *__restrict__ bins, const int *__restrict__ cnt,
-                                 int nbx, int nby, double kfac, int mult,
-                                 unsigned long long *__restrict__ bound)
+// The window along x: t = sum_k bins[bx + k] w[|k|], tc the plain count.
+__global__ void k_bound_x(const double *__restrict__ bins, const int *__restrict__ cnt,
+                          BoundAxis ax, int nby, double *__restrict__ t, int *__restrict__ tc)
 {
+    const int nbx = ax.nb;
     const int64_t nb = (int64_t)nbx * nby;
-    const int x0 = nbx >= 3 ? -1 : 0, x1 = nbx >= 2 ? 1 : 0;
-    const int y0 = nby >= 3 ? -1 : 0, y1 = nby >= 2 ? 1 : 0;
-    double best = 0.0;
-    int64_t crowd = 0;
-    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
-         b += (int64_t)gridDim.x * blockDim.x) {
-        const int bx = (int)(b / nby), by = (int)(b - (int64_t)bx * nby);
-        double sum = 0.0;
-        int64_t n = 0;
-        for (int dx = x0; dx <= x1; dx++) {
-            const int ix = wrap_index(bx + dx, nbx);
-            for (int dy = y0; dy <= y1; dy++) {
-                const int64_t k = (int64_t)ix * nby + wrap_index(by + dy, nby);
-                sum += bins[k];
-                n += cnt[k];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int bx = (int)(i / nby), by = (int)(i - (int64_t)bx * nby);
+        double s = 0.0;
+        int c = 0;
+        if (ax.full) {
+            for (int k = 0; k < nbx; k++) {
+                s += bins[(int64_t)k * nby + by];
+                c += cnt[(int64_t)k * nby + by];
+            }
+        } else {
+            for (int k = -ax.R; k <= ax.R; k++) {
+                int x = bx + k;
+                x = x < 0 ? x + nbx : (x >= nbx ? x - nbx : x);
+                s = fma(bins[(int64_t)x * nby + by], ax.w[k < 0 ? -k : k], s);
+                c += cnt[(int64_t)x * nby + by];
             }
         }
-        best = fmax(best, sum);
-        crowd = max(crowd, n);
+        t[i] = s;
+        tc[i] = c;
+    }
+}
+
+// The window along y, and the largest value over the bins.
+__global__ void k_bound_y_max(const double *__restrict__ t, const int *__restrict__ tc,
+                              BoundAxis ay, int nbx, double kfac, int mult,
+                              unsigned long long *__restrict__ bound)
+{
+    const int nby = ay.nb;
+    const int64_t nb = (int64_t)nbx * nby;
+    double best = 0.0;
+    int64_t crowd = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int bx = (int)(i / nby), by = (int)(i - (int64_t)bx * nby);
+        const double *row = t + (int64_t)bx * nby;
+        const int *rowc = tc + (int64_t)bx * nby;
+        double s = 0.0;
+        int64_t c = 0;
+        if (ay.full) {
+            for (int k = 0; k < nby; k++) {
+                s += row[k];
+                c += rowc[k];
+            }
+        } else {
+            for (int k = -ay.R; k <= ay.R; k++) {
+                int y = by + k;
+                y = y < 0 ? y + nby : (y >= nby ? y - nby : y);
+                s = fma(row[y], ay.w[k < 0 ? -k : k], s);
+                c += rowc[y];
+            }
+        }
+        best = fmax(best, s);
+        crowd = max(crowd, c);
     }
     for (int o = 16; o > 0; o >>= 1) {
         best = fmax(best, __shfl_xor_sync(~0u, best, o));
@@ -1795,6 +1882,8 @@ template __global__ void k_spread_fix_multi<2>(SpreadArgs, int, int, int64_t, in
 template __global__ void k_spread_fix_multi<3>(SpreadArgs, int, int, int64_t, int64_t, int);
 template __global__ void k_spread_fix_multi<5>(SpreadArgs, int, int, int64_t, int64_t, int);
 
+
+
 // ===========================================================================
 // 2D real FFT as two 1D complex passes (FP64 form).
 //
@@ -1859,22 +1948,29 @@ __global__ void k_unpack_real_pairs(const double2 *__restrict__ z, int nout, int
 {
     const int npair = (nout + 1) / 2;
     const int64_t n = (int64_t)npair * G;
-    unsigned long long m = 0;
+    unsigned long long m[kGmaxWords] = {0, 0, 0};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int p = (int)(i / G);
         const int64_t e = i - (int64_t)p * G;
         const double2 v = z[i];
         grid[(int64_t)(2 * p) * G + e] = v.x;
-        m = max(m, (unsigned long long)__double_as_longlong(fabs(v.x)));
+        unsigned long long mp = (unsigned long long)__double_as_longlong(fabs(v.x));
         if (2 * p + 1 < nout) {
             grid[(int64_t)(2 * p + 1) * G + e] = v.y;
-            m = max(m, (unsigned long long)__double_as_longlong(fabs(v.y)));
+            mp = max(mp, (unsigned long long)__double_as_longlong(fabs(v.y)));
         }
+#pragma unroll
+        for (int q = 0; q < kGmaxWords; q++)
+            if (q == p) m[q] = max(m[q], mp);
     }
     if (gmax) {
-        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(~0u, m, o));
-        if ((threadIdx.x & 31) == 0 && m) atomicMax(gmax, m);
+#pragma unroll
+        for (int q = 0; q < kGmaxWords; q++) {
+            unsigned long long v = m[q];
+            for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(~0u, v, o));
+            if ((threadIdx.x & 31) == 0 && v) atomicMax(gmax + q, v);
+        }
     }
 }
 
@@ -2166,8 +2262,8 @@ __global__ void k_filter_matrix_table(FilterArgs a, double *__restrict__ mtab)
 template <int NC, int PT>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs a)
 {
-    // behind k_gather_fix: runs only when the grid held a non-finite value
-    if (a.gmax && *a.gmax < kGridNonFinite) return;
+    // behind k_gather_fix: runs only when a grid held a non-finite value
+    if (a.gmax && gmax_all(a.gmax) < kGridNonFinite) return;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nt;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int P = PT > 0 ? PT : a.P;
@@ -2269,25 +2365,31 @@ __device__ __forceinline__ int grid_shift(unsigned long long gb, int Bg)
     return S < -960 ? -960 : (S > 960 ? 960 : S);
 }
 
-__global__ void k_grid_to_fixed(double *__restrict__ grid, int64_t n,
+// Grid c = blockIdx.y at its pair's scale.
+__global__ void k_grid_to_fixed(double *__restrict__ grid, int64_t G,
                                 const unsigned long long *__restrict__ gmax, int Bg)
 {
-    const unsigned long long gb = *gmax;
-    if (gb >= kGridNonFinite) return;
-    const double s = ldexp(1.0, grid_shift(gb, Bg));
-    long long *q = reinterpret_cast<long long *>(grid);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+    if (gmax_all(gmax) >= kGridNonFinite) return;
+    const int c = blockIdx.y;
+    const double s = ldexp(1.0, grid_shift(gmax[c / 2], Bg));
+    double *g = grid + (int64_t)c * G;
+    long long *q = reinterpret_cast<long long *>(g);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
          i += (int64_t)gridDim.x * blockDim.x)
-        q[i] = __double2ll_rn(grid[i] * s);
+        q[i] = __double2ll_rn(g[i] * s);
 }
 
 template <int NC, int PT>
 __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
 {
-    const unsigned long long gb = *a.gmax;
-    if (gb >= kGridNonFinite) return;
+    if (gmax_all(a.gmax) >= kGridNonFinite) return;
     const int P = PT > 0 ? PT : a.P;
-    const double outs = gb == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gb, a.Bg));
+    double outs[NC / 2];
+#pragma unroll
+    for (int k = 0; k < NC / 2; k++) {
+        const unsigned long long gb = a.gmax[k];
+        outs[k] = gb == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gb, a.Bg));
+    }
     const long long bias = P / 2 + 1;
     const long long *grid = reinterpret_cast<const long long *>(a.grid);
     const size_t G = (size_t)a.Mx * a.My;
@@ -2348,7 +2450,8 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix(GatherArgs a)
         }
 #pragma unroll
         for (int k = 0; k < NC / 2; k++)
-            a.out[k * a.nt + t] = make_double2((double)acc[2 * k] * outs, (double)acc[2 * k + 1] * outs);
+            a.out[k * a.nt + t] =
+                make_double2((double)acc[2 * k] * outs[k], (double)acc[2 * k + 1] * outs[k]);
     }
 }
 template __global__ void k_gather_fix<2, 24>(GatherArgs);
@@ -2360,9 +2463,9 @@ template __global__ void k_gather_fix<4, 0>(GatherArgs);
 
 // k_gather_fix for nr right-hand sides on one point set: a target's stencil
 // origin and Gaussian factors are formed once, then each right-hand side r
-// gathers its NC fixed-point grids (a.grid + r gstride words, scale from
-// a.gmax[r]) into a.out + r ostride.  A right-hand side whose grid held a
-// non-finite value is left to the FP64 gather.
+// gathers its NC fixed-point grids (a.grid + r gstride words, scales from
+// a.gmax + r kGmaxWords) into a.out + r ostride.  A right-hand side whose
+// grids held a non-finite value is left to the FP64 gather.
 template <int NC, int PT>
 __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int nr, int64_t gstride,
                                                              int64_t ostride)
@@ -2393,9 +2496,12 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
         }
         const bool rows_inside = my >= 0 && my + P < a.My;
         for (int r = 0; r < nr; r++) {
-            const unsigned long long gb = a.gmax[r];
-            if (gb >= kGridNonFinite) continue;      // this one runs the FP64 gather
-            const double outs = gb == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gb, a.Bg));
+            const unsigned long long *gm = a.gmax + r * kGmaxWords;
+            if (gmax_all(gm) >= kGridNonFinite) continue;   // this one runs the FP64 gather
+            double outs[NC / 2];
+#pragma unroll
+            for (int k = 0; k < NC / 2; k++)
+                outs[k] = gm[k] == 0 ? 0.0 : ldexp(a.scale, 4 - grid_shift(gm[k], a.Bg));
             const long long *grid = reinterpret_cast<const long long *>(a.grid) + r * gstride;
             long long acc[NC];
 #pragma unroll
@@ -2433,7 +2539,8 @@ __global__ void __launch_bounds__(256, 2) k_gather_fix_multi(GatherArgs a, int n
             double2 *out = a.out + r * ostride;
 #pragma unroll
             for (int k = 0; k < NC / 2; k++)
-                out[k * a.nt + t] = make_double2((double)acc[2 * k] * outs, (double)acc[2 * k + 1] * outs);
+                out[k * a.nt + t] =
+                    make_double2((double)acc[2 * k] * outs[k], (double)acc[2 * k + 1] * outs[k]);
         }
     }
 }
@@ -2557,8 +2664,8 @@ __global__ void k_filter_adj(FilterArgs a)
 template <int PT>
 __global__ void __launch_bounds__(256) k_gather_adj(GatherAdjArgs a)
 {
-    // behind k_gather_adj_ff: runs only when the grid held a non-finite value
-    if (a.gff && *a.gmax < kGridNonFinite) return;
+    // behind k_gather_adj_ff: runs only when a grid held a non-finite value
+    if (a.gff && gmax_all(a.gmax) < kGridNonFinite) return;
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.ns) return;
     const int P = PT > 0 ? PT : a.P;
@@ -2666,7 +2773,7 @@ __device__ __forceinline__ int ff_grid_shift(unsigned long long gb)
 __global__ void k_grid_to_ff(const double *__restrict__ grid, int64_t n,
                              const unsigned long long *__restrict__ gmax, float2 *__restrict__ out)
 {
-    const unsigned long long gb = *gmax;
+    const unsigned long long gb = gmax_all(gmax);    // one scale for the five grids
     if (gb >= kGridNonFinite) return;
     const double sc = ldexp(1.0, ff_grid_shift(gb));
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -2707,7 +2814,7 @@ __device__ __forceinline__ float2 shfl_xor_ff(float2 v, int o)
 template <int PT>
 __global__ void __launch_bounds__(kAdjFFWarps * 32, 2) k_gather_adj_ff(GatherAdjArgs a)
 {
-    const unsigned long long gb = *a.gmax;
+    const unsigned long long gb = gmax_all(a.gmax);
     if (gb >= kGridNonFinite) return;                // the FP64 gather runs instead
     const int sg = ff_grid_shift(gb);
     const int P = PT > 0 ? PT : a.P, P1 = P + 1;     // P1 <= 31
@@ -3355,37 +3462,20 @@ cudaError_t launch_pack_fixed_pairs(const long long *grid, int nc, int64_t G,
 cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mult, double *ws,
                                 cudaStream_t st, int64_t &launches)
 {
-    const int nbx = spread_bins(a.Mx, a.P), nby = spread_bins(a.My, a.P);
-    const int64_t nb = (int64_t)nbx * nby;
-    cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(double) * (2 * nb + 1), st);
+    const BoundAxis ax = bound_axis(a.Mx, a.P, a.a, a.h), ay = bound_axis(a.My, a.P, a.a, a.h);
+    const int64_t nb = (int64_t)ax.nb * ay.nb;
+    cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(double) * (size_t)spread_bound_words(a.Mx, a.My, a.P), st);
     if (e != cudaSuccess) return e;
-    unsigned long long *bound = reinterpret_cast<unsigned long long *>(ws + nb);
-    int *cnt = reinterpret_cast<int *>(ws + nb + 1);
+    double *bins = ws, *t = ws + nb;
+    unsigned long long *bound = reinterpret_cast<unsigned long long *>(ws + 2 * nb);
+    int *cnt = reinterpret_cast<int *>(ws + 2 * nb + 1), *tc = cnt + nb;
     if (a.ns > 0) {
-        k_spread_bin_sum<<<stream_grid(a.ns), 256, 0, st>>>(a, nc, nbx, nby, ws, cnt, bound);
+        k_spread_bin_sum<<<stream_grid(a.ns), 256, 0, st>>>(a, nc, ax.nb, ay.nb, bins, cnt, bound);
         launches++;
     }
-    k_spread_bin_max<<<stream_grid(nb), 256, 0, st>>>(ws, cnt, nbx, nby, kfac, mult, bound);
-    launches++;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_spread_fix_multi(const SpreadArgs &a, int nc, int kY, int nr, int64_t cstride,
-                                    int64_t gstride, int bstride, cudaStream_t st,
-                                    int64_t &launches)
-{
-    if (a.ns <= 0 || nr <= 0) return cudaSuccess;
-    const int64_t warps = (a.ns + 31) / 32;
-    const int64_t want = (warps + kSpreadWarps - 1) / kSpreadWarps;
-    const int64_t cap = (int64_t)sm_count() * 8;
-    const unsigned g = (unsigned)(want < cap ? want : cap);
-    switch (nc) {
-    case 2: k_spread_fix_multi<2><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
-    case 3: k_spread_fix_multi<3><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
-    case 5: k_spread_fix_multi<5><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
-    default: return cudaErrorInvalidValue;
-    }
-    launches++;
+    k_bound_x<<<stream_grid(nb), 256, 0, st>>>(bins, cnt, ax, ay.nb, t, tc);
+    k_bound_y_max<<<stream_grid(nb), 256, 0, st>>>(t, tc, ay, ax.nb, kfac, mult, bound);
+    launches += 2;
     return cudaGetLastError();
 }
 
@@ -3419,6 +3509,25 @@ cudaError_t launch_gather_fp64_fallback(const GatherArgs &a, int nc, cudaStream_
         if (a.P == 24) k_gather<4, 24><<<g, 256, 0, st>>>(a);
         else if (a.P == 12) k_gather<4, 12><<<g, 256, 0, st>>>(a);
         else k_gather<4, 0><<<g, 256, 0, st>>>(a);
+    }
+    launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spread_fix_multi(const SpreadArgs &a, int nc, int kY, int nr, int64_t cstride,
+                                    int64_t gstride, int bstride, cudaStream_t st,
+                                    int64_t &launches)
+{
+    if (a.ns <= 0 || nr <= 0) return cudaSuccess;
+    const int64_t warps = (a.ns + 31) / 32;
+    const int64_t want = (warps + kSpreadWarps - 1) / kSpreadWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const unsigned g = (unsigned)(want < cap ? want : cap);
+    switch (nc) {
+    case 2: k_spread_fix_multi<2><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    case 3: k_spread_fix_multi<3><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    case 5: k_spread_fix_multi<5><<<g, kSpreadWarps * 32, 0, st>>>(a, kY, nr, cstride, gstride, bstride); break;
+    default: return cudaErrorInvalidValue;
     }
     launches++;
     return cudaGetLastError();
@@ -3459,10 +3568,12 @@ cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, doub
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_to_fixed(double *grid, int64_t n, const unsigned long long *gmax, int Bg,
-                                 cudaStream_t st, int64_t &launches)
+cudaError_t launch_grid_to_fixed(double *grid, int nout, int64_t G, const unsigned long long *gmax,
+                                 int Bg, cudaStream_t st, int64_t &launches)
 {
-    k_grid_to_fixed<<<stream_grid(n), 256, 0, st>>>(grid, n, gmax, Bg);
+    if (nout <= 0) return cudaSuccess;
+    const dim3 grd(stream_grid(G), (unsigned)nout);
+    k_grid_to_fixed<<<grd, 256, 0, st>>>(grid, G, gmax, Bg);
     launches++;
     return cudaGetLastError();
 }

@@ -182,6 +182,34 @@ def test_fixed_spread_agrees_with_native(ft, plans, case):
     assert relerr(b1, b2) < tol, (case, "dlp", relerr(b1, b2))
 
 
+def test_integer_kspace_at_large_eta_against_oracle(ft):
+    """At eta = 3.3 (xi = 120, M = 192, P = 24) the filter's Gaussian
+    deconvolution amplifies the grid's high-frequency rounding noise by
+    about 4 orders of magnitude.  The integer spread's unit must then follow
+    the node sums, not a coarse bound: with every Gaussian factor taken as 1
+    over bins of P+2 nodes the SLP error against the oracle was 7.5e-13 and
+    the DLP's RMS-relative error 3.9e-12; with the Gaussian-weighted window
+    bound and one gather scale per output pair they are about 4e-14 and
+    5e-13 (the float-float FFTs' 2^-48 rounding, amplified the same way).
+    Bounds: SLP 1e-13, DLP 1e-12 (RMS-relative and normwise)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(41)
+    N = 20000
+    p, q = rng.random((2, N)), rng.random((2, N))
+    th = rng.random(N) * 2 * np.pi
+    n = np.vstack([np.cos(th), np.sin(th)])
+    f, g = rng.standard_normal((2, N)), rng.standard_normal((2, N))
+    prm = ft.EwaldParams.derived(120.0, 30, 30, 192, 192, 24, 1.0, 1.0)
+    assert prm.eta > 3.0
+    plan = ft.Plan(0)
+    us, ud = ft.stokes_ewald(p, q, f, g, n, prm, plan=plan)
+    plan.close()
+    rs = O.slp_ewald(p, q, f, 120.0, 30, 30, 192, 192, 1.0, 1.0, 24)[0]
+    rd = O.dlp_ewald(p, q, g, n, 120.0, 30, 30, 192, 192, 1.0, 1.0, 24)[0]
+    assert relerr(us, rs) < 1e-13, relerr(us, rs)
+    assert relerr(ud, rd) < PARITY, relerr(ud, rd)
+
+
 def test_fixed_spread_is_reproducible(ft, plans):
     """Integer sums do not depend on the order of the atomics: the k-space
     part of the FP64 form is the same bits on every call."""
