@@ -1740,6 +1740,8 @@ struct se2p_geom_st {
     float2 *spf = nullptr, *tpf = nullptr;
     int *sperm = nullptr, *tperm = nullptr, *tboxs = nullptr, *sstart = nullptr;
     int *rowptr = nullptr, *src = nullptr;
+    int *slice = nullptr;                 // slot of each 32-row slice (see launch_geom_rows)
+    int64_t nslot = 0;                    // operator slots, padding included
     float2 *cf = nullptr;
     // apply scratch (grown on demand): staged RHS and outputs
     double2 *fin = nullptr, *din = nullptr, *uout = nullptr;
@@ -1817,6 +1819,7 @@ static int geom_build(se2p_geom g, const double *psrc, const double *ptar, const
     CKS(geom_alloc(g, ntz, &g->tboxs));
     CKS(geom_alloc(g, (size_t)nbox + 1, &g->sstart));
     CKS(geom_alloc(g, ntz + 1, &g->rowptr));
+    CKS(geom_alloc(g, (ntz + 31) / 32 + 1, &g->slice));
     // wrap, then sort into the real-space boxes
     double2 *ws = nullptr, *wt = nullptr;
     int *sbox, *srank, *tbox, *trank, *count, *tstart;
@@ -1872,16 +1875,28 @@ static int geom_build(se2p_geom g, const double *psrc, const double *ptar, const
     CK(cudaStreamSynchronize(st));
     if (nnz < 0) return fail(pl, SE2P_ERR_UNSUPPORTED, "geometry: more than 2^31-1 pairs");
     g->nnz = nnz;
-    const size_t nz = (size_t)(nnz > 0 ? nnz : 1);
+    // slices of 32 rows, each padded to its longest row
+    const int64_t nsl = (nt + 31) / 32;
+    int nslot = 0;
+    if (nt > 0) {
+        CK(launch_geom_slices(g->rowptr, nt, rowcnt, st, pl->launches));
+        CK(launch_scan(rowcnt, (int)nsl, g->slice, st, pl->launches));
+        CK(cudaMemcpyAsync(&nslot, g->slice + nsl, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (nslot < 0) return fail(pl, SE2P_ERR_UNSUPPORTED, "geometry: more than 2^31-1 slots");
+    g->nslot = nslot;
+    const size_t nz = (size_t)(nslot > 0 ? nslot : 1);
     CKS(geom_alloc(g, nz, &g->src));
     CKS(geom_alloc(g, 7 * nz, &g->cf));
     int *tgt = nullptr;
     unsigned char *meta = nullptr;
     CKS(ensure_t(pl, S_GTGT, nz, &tgt));
     CKS(ensure_t(pl, S_GMETA, nz, &meta));
-    CK(launch_geom_rows(ra, g->slp, g->dlp, true, nullptr, g->rowptr, g->src, tgt, meta, st,
+    CK(cudaMemsetAsync(tgt, 0xff, sizeof(int) * nz, st));   // padding slots: tgt = -1
+    CK(launch_geom_rows(ra, g->slp, g->dlp, true, nullptr, g->slice, g->src, tgt, meta, st,
                         pl->launches));
-    CK(launch_geom_coef(ra, g->slp, g->dlp, nnz, g->src, tgt, meta, g->cf, st, pl->launches));
+    CK(launch_geom_coef(ra, g->slp, g->dlp, nslot, g->src, tgt, meta, g->cf, st, pl->launches));
     CK(cudaStreamSynchronize(st));
     return SE2P_OK;
 }
@@ -2137,14 +2152,16 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
         CK(cudaStreamWaitEvent(pl->side, pl->fork, 0));
         {
             StageTimer tm(pl, T_REAL, pl->side);
-            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nnz, g->rowptr, g->src, g->cf, cff, ncf,
-                                 doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nslot, g->rowptr, g->slice, g->src, g->cf,
+                                 cff, ncf, doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
                                  (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, pl->side, pl->launches));
         }
         CK(cudaEventRecord(pl->join, pl->side));
         double2 *uk = nullptr, *zm = nullptr, *part = nullptr;
         const int nk2 = (g->slp ? 1 : 0) + (g->dlp ? 1 : 0);
         CKS(ensure_t(pl, S_MUK, (size_t)kBatch * nk2 * nt, &uk));
+        // (on the plan's stream: on the high-priority stream beside the
+        // operator product it ran 3 % slower, both being bound by L1 and L2)
         CKS(geom_kspace_multi(g, nb, coef, (int64_t)nc * (int64_t)nsz, st, uk));
         if (g->dlp) {
             CKS(ensure_t(pl, S_ZPART, (size_t)kZeroModeParts, &part));
@@ -2181,8 +2198,8 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
         }
         {
             StageTimer tm(pl, T_REAL);
-            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nnz, g->rowptr, g->src, g->cf, cff, ncf,
-                                 doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+            CK(launch_geom_apply(g->slp, g->dlp, nt, g->nslot, g->rowptr, g->slice, g->src, g->cf,
+                                 cff, ncf, doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
                                  (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, st, pl->launches));
         }
         // k space (and the DLP zero mode and sign) per RHS through the drivers'

@@ -437,14 +437,20 @@ void fft_rows_ff_twiddles(int L, float4 *host);   // exp(-2 pi i m/L), m < L, fl
 cudaError_t launch_fft_rows_ff(double2 *data, int64_t rows, const FftRowsFF &p, const float4 *tw,
                                cudaStream_t st, int64_t &launches);
 // Real-space operator of a fixed geometry (se2p_geom.cu).
+// Rows sliced by 32 targets: entry k of row t at slice[t / 32] + 32 k + t % 32
+// (slice = exclusive scan of launch_geom_slices' slots per slice); the
+// operator arrays hold slice[ceil(nt / 32)] slots, padding marked by tgt < 0.
 cudaError_t launch_geom_rows(const RealArgs &a, bool slp, bool dlp, bool fill, int *rowcnt,
-                             const int *rowptr, int *src, int *tgt, unsigned char *meta,
+                             const int *slice, int *src, int *tgt, unsigned char *meta,
                              cudaStream_t st, int64_t &launches);
+cudaError_t launch_geom_slices(const int *rowptr, int64_t nt, int *slen, cudaStream_t st,
+                               int64_t &launches);
 cudaError_t launch_geom_coef(const RealArgs &a, bool slp, bool dlp, int64_t nnz, int *src,
                              const int *tgt, const unsigned char *meta, float2 *cf,
                              cudaStream_t st, int64_t &launches);
 cudaError_t launch_geom_apply(bool slp, bool dlp, int64_t nt, int64_t nnz, const int *rowptr,
-                              const int *src, const float2 *cf, const float2 *cff, int ncf,
+                              const int *slice, const int *src, const float2 *cf,
+                              const float2 *cff, int ncf,
                               int doff, int64_t rstride, const double *cfd_rhs, int nc,
                               int doffd, int64_t rstrided, int nr, double2 *ur_slp,
                               double2 *ur_dlp, cudaStream_t st, int64_t &launches);
