@@ -28,6 +28,11 @@ using namespace se2p;
 
 namespace {
 
+#ifndef SE2P_PATCH_NODES
+#define SE2P_PATCH_NODES 48
+#endif
+constexpr double kPatchNodes = SE2P_PATCH_NODES;   // side of a gather patch, in grid nodes
+
 enum Slot {
     S_IN_PS, S_IN_PT, S_IN_F, S_IN_FD, S_IN_N,   // staged inputs
     S_WPS, S_WPT,                               // wrapped positions
@@ -48,6 +53,7 @@ enum Slot {
     S_MTAB,                                     // cached per-mode filter multipliers
     S_PROBE,                                    // the atomic-rate probe's array
     S_MGRID, S_MGMAX, S_MUK, S_MZM,             // k space of several right-hand sides
+    S_GORDER, S_GPCNT, S_GPSTART,               // patch-major target order of the gather
     S_COUNT_SLOTS
 };
 
@@ -1081,7 +1087,21 @@ int run(se2p_plan pl, const Job &J, const Io &io)
         ga.gmax = gmax;
         ga.Bg = Bg;
         StageTimer tm(pl, T_GATHER, ks);
-        if (gmax) CK(launch_grid_to_fixed(grid, nout, (int64_t)G, gmax, Bg, ks, pl->launches));
+        if (gmax) {
+            CK(launch_grid_to_fixed(grid, nout, (int64_t)G, gmax, Bg, ks, pl->launches));
+            // the box-sorted targets visited patch by patch (about kPatchNodes
+            // grid nodes a side), so that a block's targets in flight share
+            // their grid lines in L1
+            const int pw = std::max(1, (int)std::lround(kPatchNodes * nx / (double)Mx));
+            const int ph = std::max(1, (int)std::lround(kPatchNodes * ny / (double)My));
+            int *order = nullptr, *pcnt = nullptr, *pst = nullptr;
+            CKS(ensure_t(pl, S_GORDER, ntz, &order));
+            CKS(ensure_t(pl, S_GPCNT, (size_t)nbox, &pcnt));
+            CKS(ensure_t(pl, S_GPSTART, (size_t)nbox + 1, &pst));
+            CK(launch_patch_order(tstart, tboxs, nt, nx, ny, pw, ph, pcnt, pst, order, ks,
+                                  pl->launches));
+            ga.order = order;
+        }
         CK(launch_gather(ga, nout, ks, pl->launches));
     }
 

@@ -341,6 +341,9 @@ struct GatherArgs {
     // that its pair's gmax and Bg give.
     const unsigned long long *gmax = nullptr;
     int Bg = 0;
+    // k_gather_fix: the order in which the sorted targets are visited (null:
+    // sorted order), from launch_patch_order
+    const int *order = nullptr;
 };
 
 // FP32-grid (mixed precision) k-space arguments (se2p_kernels_f32.cu).
@@ -401,6 +404,13 @@ cudaError_t launch_unpack_real_pairs(const double2 *z, int nout, int64_t G, doub
 // In place: each of the nout grids of G doubles becomes int64 round(g 2^Sg),
 // max|g| 2^Sg < 2^Bg over its pair (gmax[c / 2]), unless a gmax word marks a
 // non-finite value (then the grids stay as they are and the FP64 gather runs).
+// Patch-major order of box-sorted targets (boxes by nx + bx, cell list
+// tstart, box per sorted target tbox): patches of pw x ph boxes in row-major
+// order, their boxes row-major, each box's targets in sorted order.  order
+// gets nt entries; pcount and pstart nbox + 1 ints of scratch.
+cudaError_t launch_patch_order(const int *tstart, const int *tbox, int64_t nt, int nx, int ny,
+                               int pw, int ph, int *pcount, int *pstart, int *order,
+                               cudaStream_t st, int64_t &launches);
 cudaError_t launch_grid_to_fixed(double *grid, int nout, int64_t G, const unsigned long long *gmax,
                                  int Bg, cudaStream_t st, int64_t &launches);
 cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
