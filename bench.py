@@ -84,7 +84,7 @@ UNIT = "evals/s"
 C_IN, C_OUT = 5, 4
 SPREAD_RED_PER_SOURCE = (P + 1) ** 2 * C_IN
 FILTER_FLOP_PER_MODE = 60
-DRAM_BYTES = {"spread": 1.922e9, "gather": 0.276e9, "real": 0.213e9}
+DRAM_BYTES = {"spread": 1.925e9, "gather": 0.281e9, "real": 0.213e9}
 REAL_WARP_INST_PER_PAIR = 39.7     # ncu smsp__inst_executed / SLP+DLP pair evaluations
 REAL_FP32_INST_PER_EVAL = 556.0    # ncu FADD 374 + FFMA 130 + FMUL 52 thread instructions per evaluation
 GATHER_WARP_INST_PER_TARGET = 1508.0   # ncu smsp__inst_executed / targets (k_gather_fix<4,24>)
