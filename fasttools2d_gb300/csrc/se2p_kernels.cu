@@ -2340,7 +2340,8 @@ template __global__ void k_gather<4, 0>(GatherArgs);
 // The FP64 gather above issues one DFMA per stencil node and component and
 // is bound by the FP64 pipe.  Here the sums run in int64 registers.  After
 // the inverse FFT the grids become g' = round(g 2^Sg) (k_grid_to_fixed), Sg
-// chosen from the largest |g| so that |g'| < 2^Bg; the target's Gaussian
+// chosen from the largest |g| of the grid's output pair (SLP, DLP) so that
+// |g'| < 2^Bg; the target's Gaussian
 // factors are Yq[j] = round(Y[j] 2^62) and Xq[i] = round(X[i] 2^62) with
 // X[i] = exp(a (px - h (i - P/2))^2) and Y the same in y, as in the fixed
 // spread.  A column sums the high 64 bits of g' Yq[j], floor(g Y 2^(Sg-2)),
