@@ -526,7 +526,6 @@ __device__ __forceinline__ int fix_shift(unsigned long long bits)
 // and kfac = mult 2^(2 kY).  When the bound slot ends up all ones the FP64
 // spread runs (launch it behind launch_spread_fix with a.bound set) and the
 // grids hold doubles.
-int spread_bins(int M, int P);
 int64_t spread_bound_words(int Mx, int My, int P);
 int64_t spread_bound_slot(int Mx, int My, int P);
 cudaError_t launch_spread_bound(const SpreadArgs &a, int nc, double kfac, int mult, double *ws,

@@ -1529,20 +1529,19 @@ __device__ __forceinline__ long long mulhi_s_u(long long a, long long b)
 constexpr int kBoundBin = 4;      // nodes per bound bin and axis
 constexpr int kBoundMaxR = 15;
 
-int spread_bins(int M, int P)
-{
-    (void)P;
-    return (M + kBoundBin - 1) / kBoundBin;
-}
+// Bound bins along an axis of M nodes.
+static int spread_bins(int M) { return (M + kBoundBin - 1) / kBoundBin; }
 
 int64_t spread_bound_words(int Mx, int My, int P)
 {
-    return 3 * (int64_t)spread_bins(Mx, P) * spread_bins(My, P) + 1;
+    (void)P;
+    return 3 * (int64_t)spread_bins(Mx) * spread_bins(My) + 1;
 }
 
 int64_t spread_bound_slot(int Mx, int My, int P)
 {
-    return 2 * (int64_t)spread_bins(Mx, P) * spread_bins(My, P);
+    (void)P;
+    return 2 * (int64_t)spread_bins(Mx) * spread_bins(My);
 }
 
 // One axis of the bound's window: bins within R of a node's bin, and the
@@ -1556,7 +1555,7 @@ struct BoundAxis {
 static BoundAxis bound_axis(int M, int P, double a, double h)
 {
     BoundAxis ax{};
-    ax.nb = spread_bins(M, P);
+    ax.nb = spread_bins(M);
     const int slack = M % kBoundBin ? 1 : 0;
     const int R = (P / 2 + 1) / kBoundBin + 1 + slack;
     if (2 * R + 1 > ax.nb || R > kBoundMaxR) {
