@@ -2146,7 +2146,11 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
     double2 *uo_slp = g->uout, *uo_dlp = g->uout + (g->slp ? (size_t)nrhs * nt : 0);
 
     const int nc = (g->slp ? 2 : 0) + (g->dlp ? 3 : 0);
-    const int ncf = (g->slp ? 2 : 0) + (g->dlp ? 5 : 0);
+    // the stored operator reads five float-float coefficients per source and
+    // right-hand side (SLP f; DLP S11, S12+S21, S22), stored per source for
+    // the batch's right-hand sides together, [source][rhs][5]: one 40 B run
+    // per right-hand side in one contiguous block per source
+    const int ncf = nc;
     const int doff_ff = g->slp ? 2 : 0;
     constexpr int kBatch = 4;
     double *coef = nullptr;
@@ -2168,15 +2172,15 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
             const double2 *fd = g->dlp ? g->din + (size_t)(r0 + r) * ns : nullptr;
             double *cr = coef + (size_t)r * nc * nsz;
             CK(launch_src_coef(ns, g->sperm, fs, fd, g->nr, cr, nc, st, pl->launches));
-            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf * nsz, ncf,
-                                  st, pl->launches));
+            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf, ncf,
+                                  st, pl->launches, (int64_t)nb * ncf, false));
         }
         CK(cudaEventRecord(pl->fork, st));
         CK(cudaStreamWaitEvent(pl->side, pl->fork, 0));
         {
             StageTimer tm(pl, T_REAL, pl->side);
             CK(launch_geom_apply(g->slp, g->dlp, nt, g->nslot, g->rowptr, g->slice, g->src, g->cf,
-                                 cff, ncf, doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+                                 cff, nb * ncf, doff_ff, (int64_t)ncf, coef, nc, doff_ff,
                                  (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, pl->side, pl->launches));
         }
         CK(cudaEventRecord(pl->join, pl->side));
@@ -2216,13 +2220,13 @@ int se2p_geom_apply(se2p_geom g, int nrhs, const double *f_slp, const double *f_
             const double2 *fd = g->dlp ? g->din + (size_t)(r0 + r) * ns : nullptr;
             double *cr = coef + (size_t)r * nc * nsz;
             CK(launch_src_coef(ns, g->sperm, fs, fd, g->nr, cr, nc, st, pl->launches));
-            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf * nsz, ncf,
-                                  st, pl->launches));
+            CK(launch_src_coef_ff(ns, cr, nc, g->slp, g->dlp, cff + (size_t)r * ncf, ncf,
+                                  st, pl->launches, (int64_t)nb * ncf, false));
         }
         {
             StageTimer tm(pl, T_REAL);
             CK(launch_geom_apply(g->slp, g->dlp, nt, g->nslot, g->rowptr, g->slice, g->src, g->cf,
-                                 cff, ncf, doff_ff, (int64_t)ncf * (int64_t)nsz, coef, nc, doff_ff,
+                                 cff, nb * ncf, doff_ff, (int64_t)ncf, coef, nc, doff_ff,
                                  (int64_t)nc * (int64_t)nsz, nb, ur0, ur1, st, pl->launches));
         }
         // k space (and the DLP zero mode and sign) per RHS through the drivers'

@@ -387,8 +387,12 @@ cudaError_t launch_bin(const BinArgs &a, int *start, int nbox, int *perm, int *s
 cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
                             const double2 *f_dlp, const double2 *nrm, double *coef, int nc,
                             cudaStream_t st, int64_t &launches);
+// out: per source ostride float2 (ncf when 0) from out + ostride j; tails =
+// false leaves out the DLP pair 3 S11 + S22, 3 S22 + S11 (the real-space
+// kernels read it, the geometry's stored operator does not).
 cudaError_t launch_src_coef_ff(int64_t n, const double *coef, int nc, bool slp, bool dlp,
-                               float2 *out, int ncf, cudaStream_t st, int64_t &launches);
+                               float2 *out, int ncf, cudaStream_t st, int64_t &launches,
+                               int64_t ostride = 0, bool tails = true);
 cudaError_t launch_real(const RealArgs &a, bool slp, bool dlp, cudaStream_t st,
                         int64_t &launches, int form = kFormFP64);
 // 2D real FFT through 1D complex passes (se2p_kernels.cu): pack real grid

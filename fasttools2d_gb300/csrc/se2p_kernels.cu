@@ -133,12 +133,12 @@ __global__ void k_src_coef(int64_t n, const int *__restrict__ perm,
 // form: SLP f1, f2; DLP S11, S12+S21, S22 and the combinations 3 S11 + S22,
 // 3 S22 + S11 of the stresslet contraction (formed in FP64, then split).
 __global__ void k_src_coef_ff(int64_t n, const double *__restrict__ coef, int nc, int slp,
-                              int dlp, float2 *__restrict__ out, int ncf)
+                              int dlp, float2 *__restrict__ out, int64_t ostride, int tails)
 {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const double *c = coef + (int64_t)nc * j;
-    float2 *o = out + (int64_t)ncf * j;
+    float2 *o = out + ostride * j;
     if (slp) {
         o[0] = ff_split(c[0]);
         o[1] = ff_split(c[1]);
@@ -149,8 +149,10 @@ __global__ void k_src_coef_ff(int64_t n, const double *__restrict__ coef, int nc
         o[0] = ff_split(c[0]);
         o[1] = ff_split(c[1]);
         o[2] = ff_split(c[2]);
-        o[3] = ff_split(fma(3.0, c[0], c[2]));
-        o[4] = ff_split(fma(3.0, c[2], c[0]));
+        if (tails) {
+            o[3] = ff_split(fma(3.0, c[0], c[2]));
+            o[4] = ff_split(fma(3.0, c[2], c[0]));
+        }
     }
 }
 
@@ -3210,10 +3212,12 @@ cudaError_t launch_src_coef(int64_t n, const int *perm, const double2 *f_slp,
 }
 
 cudaError_t launch_src_coef_ff(int64_t n, const double *coef, int nc, bool slp, bool dlp,
-                               float2 *out, int ncf, cudaStream_t st, int64_t &launches)
+                               float2 *out, int ncf, cudaStream_t st, int64_t &launches,
+                               int64_t ostride, bool tails)
 {
     if (n <= 0) return cudaSuccess;
-    k_src_coef_ff<<<grid_for(n, 256), 256, 0, st>>>(n, coef, nc, slp, dlp, out, ncf);
+    k_src_coef_ff<<<grid_for(n, 256), 256, 0, st>>>(n, coef, nc, slp, dlp, out,
+                                                     ostride > 0 ? ostride : ncf, tails ? 1 : 0);
     launches++;
     return cudaGetLastError();
 }
