@@ -1497,12 +1497,12 @@ template __global__ void k_spread<5>(SpreadArgs);
 // bin sums weighted by those largest factors, a separable window of 2R + 1
 // bins per axis, bound every node's sum; its largest value, times 2^(2 kY)
 // and the number of times one stencil covers a node when M <= P, is the
-// bound.  (Bins of P+2 nodes with every factor taken as 1 bounded the sums
-// about 50 times too high; the unit 2^-S scales with the bound, and its
-// rounding noise, white on the grid, is amplified by the deconvolution of the
-// Gaussian in the filter: at eta = 3.3 it reached 3e-13 of the k-space
-// velocity.)  Where the window would wrap onto itself (grids under 2R + 1
-// bins) every bin counts with factor 1.
+// bound, about 5 times the largest node sum on uniform points.  (Bins of P+2
+// nodes with every factor taken as 1 gave about 170 times it.  The unit 2^-S
+// scales with the bound, and its rounding noise, white on the grid, is
+// amplified by the deconvolution of the Gaussian in the filter: at eta = 3.3
+// it reached 3e-13 of the k-space velocity.)  Where the window would wrap
+// onto itself (grids under 2R + 1 bins) every bin counts with factor 1.
 //
 // The unit 2^-S is fixed by that bound, i.e. by sum |c|, while FP64 atomics
 // round relative to the partial sums, which grow like sqrt(n) when the signs
