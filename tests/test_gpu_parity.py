@@ -164,6 +164,35 @@ def test_argument_errors(ft, plan):
     assert relerr(u, g["out_slp_real"]) < PARITY
 
 
+def test_pending_runtime_error_of_other_code_is_not_reported(ft, plan):
+    """An error that other code left pending in the CUDA runtime (here an
+    invalid device ordinal from cudaSetDevice, which touches no GPU state) is
+    not this library's: the next call clears it on entry and succeeds.  Its
+    launch checks read cudaGetLastError, so without that the call reported the
+    other code's error as its own."""
+    import ctypes
+    import ctypes.util
+    names = ["libcudart.so.13", "libcudart.so.12", ctypes.util.find_library("cudart")]
+    rt = None
+    for name in filter(None, names):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    if rt is None:
+        pytest.skip("libcudart not loadable")
+    g = load_golden(golden_names()[0])
+    ps, pt, f = g["psrc"], g["ptar"], g["f"]
+    ref = ft.mex_stokes_slp_real(ps, pt, f, g["xi"], g["nside_x"], g["nside_y"], g["Lx"], g["Ly"],
+                                 plan=plan)
+    assert rt.cudaSetDevice(ctypes.c_int(1 << 20)) != 0        # left pending
+    got = ft.mex_stokes_slp_real(ps, pt, f, g["xi"], g["nside_x"], g["nside_y"], g["Lx"], g["Ly"],
+                                 plan=plan)                       # does not raise
+    # (not bitwise: the within-box order of the sort comes from atomics)
+    assert relerr(got, ref) < 1e-13
+
+
 def test_matlab_driver_stresslet_identity(ft, plan):
     """stresslet_identity_test.m through StokesDLP_ewald_2p (parameters chosen by the driver)."""
     r, L, ns, nt = 1.0, 4.0, 256, 16
