@@ -668,6 +668,10 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
     const int H1 = My / 2 + 1, ncg = (nc + 1) / 2;
     const size_t G = (size_t)Mx * My;
     double2 *zgd = reinterpret_cast<double2 *>(zg);
+    // an odd plane count's last plane goes in as half as many rows, its rows x
+    // and x + Mx/2 in one complex row (the pair's imaginary half is otherwise
+    // zero): 2.5 instead of 3 grids of y transforms for SLP+DLP
+    const bool fold = ff && (nc & 1) && Mx % 2 == 0;
     if (ff) {
         // the pack is fused into the float-float y pass
         FftRowsFF io;
@@ -676,7 +680,9 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
         io.pack_in = grid;
         io.bound = fixb;
         io.npl_in = nc;
-        CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1, &io));
+        io.fold = fold ? 1 : 0;
+        const int64_t rows = fold ? (int64_t)(nc / 2) * Mx + Mx / 2 : (int64_t)ncg * Mx;
+        CKS(fft_rows(pl, ks, ff, Mx, My, My, rows, 4, zgd, -1, &io));
     } else {
         if (fixb)
             CK(launch_pack_fixed_pairs(reinterpret_cast<const long long *>(grid), nc, (int64_t)G,
@@ -686,7 +692,7 @@ static int fft_fwd_1d(se2p_plan pl, cudaStream_t ks, int Mx, int My, const doubl
         CKS(fft_rows(pl, ks, ff, Mx, My, My, (int64_t)ncg * Mx, 4, zgd, -1));
     }
     CK(launch_split_half_spectra_t(zgd, nc, Mx, My, reinterpret_cast<double2 *>(spec), ks,
-                                   pl->launches));
+                                   pl->launches, fold));
     CKS(fft_rows(pl, ks, ff, Mx, My, Mx, (int64_t)nc * H1, 6, reinterpret_cast<double2 *>(spec), -1));
     return SE2P_OK;
 }

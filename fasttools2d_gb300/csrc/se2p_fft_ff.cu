@@ -342,11 +342,15 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
     for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
         double2 *d = data + row * L;
         const int64_t q = p.Mx ? row / p.Mx : 0, xr = row - q * p.Mx;
-        const int64_t off_re = (2 * q) * p.G + xr * L, off_im = (2 * q + 1) * p.G + xr * L;
+        int64_t off_re = (2 * q) * p.G + xr * L, off_im = (2 * q + 1) * p.G + xr * L;
+        bool has_im = 2 * q + 1 < p.npl_in;
+        if (p.fold && 2 * q + 1 == p.npl_in) {        // the folded plane: rows xr, xr + Mx/2
+            off_im = (2 * q) * p.G + (xr + p.Mx / 2) * L;
+            has_im = true;
+        }
         int e;
         if (fixed_in) {
             const long long *g = static_cast<const long long *>(p.pack_in);
-            const bool has_im = 2 * q + 1 < p.npl_in;
             for (int k = threadIdx.x; k < L; k += blockDim.x) {
                 const long long vr = g[off_re + k], vi = has_im ? g[off_im + k] : 0;
                 sh_put(A, Lp, k, fc{ll_to_ff(vr), ll_to_ff(vi)});
@@ -361,7 +365,7 @@ __global__ void __launch_bounds__(256) k_fft_rows_ff(double2 *__restrict__ data,
                 double2 v;
                 if (p.pack_in) {
                     const double *g = static_cast<const double *>(p.pack_in);
-                    v = make_double2(g[off_re + k], 2 * q + 1 < p.npl_in ? g[off_im + k] : 0.0);
+                    v = make_double2(g[off_re + k], has_im ? g[off_im + k] : 0.0);
                 } else {
                     v = d[k];
                 }

@@ -417,8 +417,10 @@ cudaError_t launch_patch_order(const int *tstart, const int *tbox, int64_t nt, i
                                cudaStream_t st, int64_t &launches);
 cudaError_t launch_grid_to_fixed(double *grid, int nout, int64_t G, const unsigned long long *gmax,
                                  int Bg, cudaStream_t st, int64_t &launches);
+// fold: the last pair of an odd nc holds plane nc-1's rows x (re) and x + Mx/2
+// (im) as its rows x < Mx/2 (FftRowsFF::fold).
 cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
-                                        cudaStream_t st, int64_t &launches);
+                                        cudaStream_t st, int64_t &launches, bool fold = false);
 cudaError_t launch_join_half_spectra_t(const double2 *specT, int nout, int Mx, int My, double2 *z,
                                        cudaStream_t st, int64_t &launches);
 // Float-float row FFTs (se2p_fft_ff.cu): unnormalised C2C of `rows`
@@ -442,6 +444,9 @@ struct FftRowsFF {
     const void *pack_in = nullptr;    // int64 planes at scale 2^S (bound), or doubles
     const unsigned long long *bound = nullptr;   // spread bound slot; null or all ones: doubles
     int npl_in = 0;
+    // an odd plane count's last plane folded: its rows x and x + Mx/2 form
+    // complex row x of its pair (Mx/2 rows instead of Mx half-empty ones)
+    int fold = 0;
     double *unpack_out = nullptr;     // double planes
     int npl_out = 0;
     unsigned long long *gmax = nullptr;   // largest |value| unpacked per pair q (bit pattern), optional

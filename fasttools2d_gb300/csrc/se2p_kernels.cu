@@ -1982,7 +1982,8 @@ constexpr int kTT = 32;
 
 __global__ void __launch_bounds__(256) k_split_half_spectra_t(const double2 *__restrict__ z,
                                                               int nc, int Mx, int My,
-                                                              double2 *__restrict__ specT)
+                                                              double2 *__restrict__ specT,
+                                                              int fold)
 {
     __shared__ double2 sa[kTT][kTT + 1], sb[kTT][kTT + 1];
     const int H1 = My / 2 + 1;
@@ -1990,10 +1991,13 @@ __global__ void __launch_bounds__(256) k_split_half_spectra_t(const double2 *__r
     const int ky0 = blockIdx.x * kTT, x0 = blockIdx.y * kTT, p = blockIdx.z;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
     const double2 *zp = z + (int64_t)p * G;
+    // a folded pair: rows x < Mx/2 hold plane 2p's rows x and x + Mx/2
+    const bool folded = fold && 2 * p + 1 == nc;
+    const int xend = folded ? Mx / 2 : Mx;
     // load: lanes along ky
     for (int r = ty; r < kTT; r += 8) {
         const int x = x0 + r, ky = ky0 + tx;
-        if (x < Mx && ky < H1) {
+        if (x < xend && ky < H1) {
             const double2 zk = zp[(int64_t)x * My + ky];
             const double2 zm = zp[(int64_t)x * My + (ky == 0 ? 0 : My - ky)];
             sa[tx][r] = make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
@@ -2004,9 +2008,12 @@ __global__ void __launch_bounds__(256) k_split_half_spectra_t(const double2 *__r
     // store: lanes along x
     for (int r = ty; r < kTT; r += 8) {
         const int ky = ky0 + r, x = x0 + tx;
-        if (x < Mx && ky < H1) {
+        if (x < xend && ky < H1) {
             specT[(int64_t)(2 * p) * HT + (int64_t)ky * Mx + x] = sa[r][tx];
-            if (2 * p + 1 < nc) specT[(int64_t)(2 * p + 1) * HT + (int64_t)ky * Mx + x] = sb[r][tx];
+            if (folded)
+                specT[(int64_t)(2 * p) * HT + (int64_t)ky * Mx + x + Mx / 2] = sb[r][tx];
+            else if (2 * p + 1 < nc)
+                specT[(int64_t)(2 * p + 1) * HT + (int64_t)ky * Mx + x] = sb[r][tx];
         }
     }
 }
@@ -3657,11 +3664,11 @@ cudaError_t launch_scan(const int *count, int n, int *start, cudaStream_t st, in
 namespace se2p {
 
 cudaError_t launch_split_half_spectra_t(const double2 *z, int nc, int Mx, int My, double2 *specT,
-                                        cudaStream_t st, int64_t &launches)
+                                        cudaStream_t st, int64_t &launches, bool fold)
 {
     const int H1 = My / 2 + 1;
     const dim3 g((H1 + kTT - 1) / kTT, (Mx + kTT - 1) / kTT, (nc + 1) / 2);
-    k_split_half_spectra_t<<<g, 256, 0, st>>>(z, nc, Mx, My, specT);
+    k_split_half_spectra_t<<<g, 256, 0, st>>>(z, nc, Mx, My, specT, fold && (nc & 1) ? 1 : 0);
     launches++;
     return cudaGetLastError();
 }
