@@ -127,9 +127,11 @@ def test_ff_adjoint_agrees_with_native(ft, plans, N, xi, nside, M):
 # grids no wider than the stencil (a stencil covering a node several times).
 # Beyond 2^14 stencil covers in a 3 x 3 bin neighbourhood the FP64 form
 # switches to FP64 atomics on the device ("crowded" cases), where it agrees
-# with the native form to rounding.
+# with the native form to rounding.  Both forms then sum in the order the
+# atomics land, which changes from run to run: on the 30000-point cluster
+# (std 0.001) the SLP difference was 6e-15 to 1.1e-14 over runs.
 KSPACE_FIX_VS_NATIVE = 1e-13
-KSPACE_CROWDED_VS_NATIVE = 1e-14
+KSPACE_CROWDED_VS_NATIVE = 5e-14
 
 
 def _kspace_pair(ft, plans, p, q, f, n, xi, eta, M, w, P):
