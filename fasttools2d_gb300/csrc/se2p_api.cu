@@ -5,7 +5,7 @@
 // One evaluation runs as
 //   [wrap] -> sort sources/targets into boxes -> per-source coefficients
 //   -> real space (k_real)                     \  both read the sorted data
-//   -> spread -> D2Z -> filter -> Z2D -> gather /
+//   -> spread -> 2D FFT -> filter -> inverse FFT -> gather /
 //   -> [DLP zero mode] -> assemble in the caller's target order.
 #include <cuda_runtime.h>
 #include <cufft.h>

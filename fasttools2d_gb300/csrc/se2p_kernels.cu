@@ -2,13 +2,16 @@
 // (SE) summation of the 2D Stokeslet (SLP) and stresslet (DLP).
 //
 // The reference (FastTools2D, PeriodicEwald/src/mex) runs these loops on the
-// CPU with OpenMP; here each is a GB300 kernel.  All arithmetic is FP64.
-// GB300 issues about 2 FP64 FMA per clock per SM (1/58 of its FP32 rate), so
-// the kernels are organised to keep every FP64 warp instruction fully
-// populated: accepted real-space pairs are compacted before the Pade/exp
-// work, the spread walks a flattened (P+1)^2 stencil, and the gather gives
-// each lane its own target.  Index, compare and shuffle work is nearly free
-// next to the FP64 pipe.
+// CPU with OpenMP; here each is a GB300 kernel.  GB300 issues about 2 FP64
+// FMA per clock per SM, some 70 times fewer than FP32, so each stage of the
+// default form runs in the narrowest arithmetic that keeps results within
+// 1e-12 of the reference: real-space far pairs in float-float on the FP32
+// pipe (near pairs, the self term and the cutoff decisions in FP64), the
+// spread and gather as exact int64 sums of rounded products, the filter in
+// FP64.  The all-FP64 versions of these kernels serve the FP64_NATIVE form
+// and the fallbacks; they keep every FP64 warp instruction fully populated
+// (accepted pairs compacted before the Pade/exp work, a flattened (P+1)^2
+// stencil per spread source, one gather target per lane).
 #include "se2p_internal.cuh"
 
 #include <algorithm>
