@@ -264,8 +264,6 @@ struct RealWarp {
     double2 nbz[9];
     float2 nbzf[9];
     float2 nbe[9];              // 2^-22 (|t| + |z|) per neighbour box (the pre-test band)
-    // FP32-grid form: target position as float-float (hi.x, hi.y, lo.x, lo.y)
-    float4 tposff[kRing];
 };
 
 // Segmented warp reduction of (v0..v3) by nondecreasing key; the last lane
@@ -447,7 +445,8 @@ __constant__ float c_e1f[3][22] = {
 // A pair in FP32 (mixed-precision form, far pairs): the offsets are formed in
 // FP64 in each kernel's own order, then everything runs in FP32.
 template <bool SLP, bool DLP>
-__device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp &W, int2 e,
+__device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp &W,
+                                              const float4 *tposff, int2 e,
                                               const float *e1f, const float4 &zxf,
                                               const float4 &zyf, float &s1, float &s2, float &d1,
                                               float &d2)
@@ -461,7 +460,7 @@ __device__ __forceinline__ void real_pair_f32(const RealArgs &a, const RealWarp 
     // within a factor of 2 across a periodic image), and the low-order terms
     // follow; one rounding to FP32 at the end.
     const float2 Sh = a.spf[s], Sl = a.spl[s];
-    const float4 Tq = W.tposff[slot];
+    const float4 Tq = tposff[slot];
     const float2 zx = ux < 0 ? make_float2(zxf.x, zxf.y)
                              : (ux >= a.nx ? make_float2(zxf.z, zxf.w) : make_float2(0.f, 0.f));
     const float2 zy = uy < 0 ? make_float2(zyf.x, zyf.y)
@@ -590,15 +589,21 @@ __global__ void __launch_bounds__(kRealWarps * 32, SE2P_REAL_MINB) k_real(RealAr
 {
     constexpr bool MIXED = FORM == kFormF32;
     constexpr bool FF = FORM == kFormFF;
+    // Shared arrays of one form only are sized 1 in the others: the
+    // float-float form's 6 blocks per SM then fit the 132 KB shared-memory
+    // carve-out, which leaves more of the SM's L1 to the source reads.
     __shared__ RealWarp warps[kRealWarps];
     __shared__ double tab[64];
-    __shared__ float2 tabff[64];
+    __shared__ float2 tabff[FF ? 64 : 1];
     __shared__ double e1s[66];
-    __shared__ float e1f[66];
+    __shared__ float e1f[MIXED ? 66 : 1];
+    // FP32-grid form: target positions as float-float (hi.x, hi.y, lo.x, lo.y)
+    __shared__ float4 tposff_s[kRealWarps][MIXED ? kRing : 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float4 *tposff = tposff_s[wid];
     for (int i = threadIdx.x; i < 64; i += blockDim.x) {
         tab[i] = c_exp_tab[i];
-        tabff[i] = ff_split(c_exp_tab[i]);
+        if (FF) tabff[i] = ff_split(c_exp_tab[i]);
     }
     const float2 xi2ff = ff_split(a.xi2), pfff = ff_split(a.pf);
     // image shifts as float-float, for the FP32-grid form's offsets
@@ -612,7 +617,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, SE2P_REAL_MINB) k_real(RealAr
     const float xlo = FF ? 1.0001f : 1.0f, xhi = FF ? 63.9f : INFINITY;
     for (int i = threadIdx.x; i < 66; i += blockDim.x) {
         e1s[i] = (&c_e1[0][0])[i];
-        e1f[i] = (&c_e1f[0][0])[i];
+        if (MIXED) e1f[i] = (&c_e1f[0][0])[i];
     }
     __syncthreads();
     RealWarp &W = warps[wid];
@@ -661,7 +666,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, SE2P_REAL_MINB) k_real(RealAr
             }
         }
         if (lane < cnt) {
-            if (f32) real_pair_f32<SLP, DLP>(a, W, e, e1f, zxf, zyf, P.f1, P.f2, P.g1, P.g2);
+            if (f32) real_pair_f32<SLP, DLP>(a, W, tposff, e, e1f, zxf, zyf, P.f1, P.f2, P.g1, P.g2);
             else if (ffp)
                 real_pair_ff<SLP, DLP>(a, W, e, tabff, xi2ff, pfff, P.h1, P.h2, P.k1, P.k2);
             else real_pair<SLP, DLP>(a, W, e, tab, e1s, P.s1, P.s2, P.d1, P.d2);
@@ -740,7 +745,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, SE2P_REAL_MINB) k_real(RealAr
             W.tidx[slot] = t;
             if (MIXED) {
                 const float2 tl = a.tpl[t];
-                W.tposff[slot] = make_float4(Tf.x, Tf.y, tl.x, tl.y);
+                tposff[slot] = make_float4(Tf.x, Tf.y, tl.x, tl.y);
             }
         }
         // neighbour boxes: first source, counts -> list prefix, image shift
