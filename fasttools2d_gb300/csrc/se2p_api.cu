@@ -1241,7 +1241,6 @@ int run_adjoint(se2p_plan pl, const Job &J, const AdjIo &io)
 
     // real space (side stream) ...
     RealArgs ra{};
-    memset(&ra, 0, sizeof ra);
     ra.sp = sp;
     ra.spf = spf;
     ra.coef = coef;
