@@ -114,6 +114,45 @@ def _structure(k1, k2, xs, ys, weights, chunk=512):
     return out
 
 
+def _structure_grid(Lx, Ly, kinf, xs, ys, weights, chunk=4096):
+    """_structure on the full mode grid, in _modes' order (k = 0 removed),
+    as sums over source chunks of (X w) Y^T with X[a, s] = exp(i k1_a x_s) and
+    Y[b, s] = exp(i k2_b y_s): the phases factor per axis, so the cost is two
+    small exponential tables and one matrix product per chunk instead of one
+    exponential per mode and source."""
+    j = np.arange(-kinf + 1, kinf + 1)
+    out = [np.zeros((j.size, j.size), complex) for _ in weights]
+    for s0 in range(0, xs.size, chunk):
+        X = np.exp(1j * (2 * np.pi / Lx) * np.outer(j, xs[s0:s0 + chunk]))
+        Y = np.exp(1j * (2 * np.pi / Ly) * np.outer(j, ys[s0:s0 + chunk]))
+        for o, w in zip(out, weights):
+            o += (X * w[s0:s0 + chunk]) @ Y.T
+    keep = np.ones(j.size * j.size, bool)
+    keep[(kinf - 1) * j.size + (kinf - 1)] = False          # j1 = j2 = 0
+    return [o.ravel()[keep] for o in out]
+
+
+def _evaluate_grid(Lx, Ly, kinf, coefs, xt, yt, chunk=4096):
+    """_evaluate for coefficients in _modes' order (k = 0 removed), through
+    per-axis phase tables: u(t) = Re sum_a X_t[a] (C Y_t)[a]."""
+    j = np.arange(-kinf + 1, kinf + 1)
+    n = j.size
+    u = np.zeros((len(coefs), xt.size))
+    grids = []
+    for co in coefs:
+        g = np.zeros(n * n, complex)
+        keep = np.ones(n * n, bool)
+        keep[(kinf - 1) * n + (kinf - 1)] = False
+        g[keep] = co
+        grids.append(g.reshape(n, n))
+    for t0 in range(0, xt.size, chunk):
+        X = np.exp(-1j * (2 * np.pi / Lx) * np.outer(j, xt[t0:t0 + chunk]))
+        Y = np.exp(-1j * (2 * np.pi / Ly) * np.outer(j, yt[t0:t0 + chunk]))
+        for c, g in enumerate(grids):
+            u[c, t0:t0 + chunk] = np.einsum("at,at->t", X, g @ Y).real
+    return u
+
+
 def _evaluate(k1, k2, coefs, xt, yt, chunk=512):
     """u_c(t) = Re sum_k coefs_c(k) exp(-i k.x_t)."""
     u = np.zeros((len(coefs), xt.size))
@@ -124,21 +163,37 @@ def _evaluate(k1, k2, coefs, xt, yt, chunk=512):
     return u
 
 
-def slp_kspace_ds(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, xi, kinf=None):
+def _sums(Lx, Ly, kinf, k1, k2, xs, ys, weights, grid):
+    if grid:
+        return _structure_grid(Lx, Ly, kinf, xs, ys, weights)
+    return _structure(k1, k2, xs, ys, weights)
+
+
+def _values(Lx, Ly, kinf, k1, k2, coefs, xt, yt, grid):
+    if grid:
+        return _evaluate_grid(Lx, Ly, kinf, coefs, xt, yt)
+    return _evaluate(k1, k2, coefs, xt, yt)
+
+
+def slp_kspace_ds(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, xi, kinf=None, grid=False):
+    """grid=True sums the same modes through per-axis phase tables (for
+    thousands of sources and modes)."""
     if kinf is None:
         kinf = default_kinf(xi, Lx, Ly)
     k1, k2 = _modes(Lx, Ly, kinf)
     K2 = k1 * k1 + k2 * k2
     A = (1 + K2 / (4 * xi * xi)) * np.exp(-K2 / (4 * xi * xi)) / K2
-    F1, F2 = _structure(k1, k2, np.asarray(xsrc), np.asarray(ysrc),
-                        [np.asarray(f1, float), np.asarray(f2, float)])
+    F1, F2 = _sums(Lx, Ly, kinf, k1, k2, np.asarray(xsrc, float), np.asarray(ysrc, float),
+                   [np.asarray(f1, float), np.asarray(f2, float)], grid)
     # (f - k (k.f)/k^2) A: stokeslet_k_sum, stokes_slp_kspace_ds.m:67-74
     c1 = A * ((1 - k1 * k1 / K2) * F1 - k1 * k2 / K2 * F2)
     c2 = A * (-k1 * k2 / K2 * F1 + (1 - k2 * k2 / K2) * F2)
-    return _evaluate(k1, k2, [c1, c2], np.asarray(xtar), np.asarray(ytar)) / (Lx * Ly)
+    return _values(Lx, Ly, kinf, k1, k2, [c1, c2], np.asarray(xtar, float),
+                   np.asarray(ytar, float), grid) / (Lx * Ly)
 
 
-def dlp_kspace_ds(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, xi, kinf=None):
+def dlp_kspace_ds(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, xi, kinf=None, grid=False):
+    """grid=True as for slp_kspace_ds."""
     if kinf is None:
         kinf = default_kinf(xi, Lx, Ly)
     xsrc, ysrc, n1, n2, f1, f2 = map(lambda a: np.asarray(a, float),
@@ -147,8 +202,8 @@ def dlp_kspace_ds(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, xi, kinf=None)
     K2 = k1 * k1 + k2 * k2
     B = (1 + K2 / (4 * xi * xi)) * np.exp(-K2 / (4 * xi * xi)) / K2
     # S_ab = f_a n_b per source, summed into structure factors.
-    S11, S12, S21, S22 = _structure(k1, k2, xsrc, ysrc,
-                                    [f1 * n1, f1 * n2, f2 * n1, f2 * n2])
+    S11, S12, S21, S22 = _sums(Lx, Ly, kinf, k1, k2, xsrc, ysrc,
+                               [f1 * n1, f1 * n2, f2 * n1, f2 * n2], grid)
     # stokes_dlp_k_sum (stokes_dlp_kspace_ds.m:73-85), linear in S_ab:
     #   f1 (k.n) = k1 S11 + k2 S12 ; n1 (k.f) = k1 S11 + k2 S21 ; k1 (f.n) = k1 (S11 + S22)
     #   (k.n)(k.f) = k1^2 S11 + k1 k2 (S12 + S21) + k2^2 S22
@@ -156,7 +211,8 @@ def dlp_kspace_ds(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, xi, kinf=None)
     fn = S11 + S22
     g1 = (k1 * S11 + k2 * S12) + (k1 * S11 + k2 * S21) + k1 * fn - 2 * k1 * kk / K2
     g2 = (k1 * S21 + k2 * S22) + (k1 * S12 + k2 * S22) + k2 * fn - 2 * k2 * kk / K2
-    u = _evaluate(k1, k2, [1j * B * g1, 1j * B * g2], np.asarray(xtar), np.asarray(ytar))
+    u = _values(Lx, Ly, kinf, k1, k2, [1j * B * g1, 1j * B * g2], np.asarray(xtar, float),
+                np.asarray(ytar, float), grid)
     u /= (Lx * Ly)
     fdotn = f1 * n1 + f2 * n2
     u[0] -= np.sum(fdotn * xsrc) / (Lx * Ly)
